@@ -1,0 +1,112 @@
+"""ctypes binding of libaeroflux_cuda (include/aeroflux_cuda.h).
+
+The library is built in-tree by aeroflux_gb300/build.py.  There is no CPU
+fallback: if the shared library is missing or fails to load, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libaeroflux_cuda.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "aeroflux_cuda.h")
+
+AF_OK = 0
+AF_ERR_CONFIG = -1
+AF_ERR_CUDA = -2
+AF_ERR_FAULT = -3
+AF_ERR_ARG = -4
+AF_ERR_UNSUPPORTED = -5
+AF_ERR_CLOSED = -6
+AF_ERR_NOMEM = -7
+
+AF_PRECISION_FP64 = 0
+AF_PRECISION_MIXED = 1
+
+
+class AfConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
+        ("ghost", C.c_int64),
+        ("h", C.c_double), ("viscosity", C.c_double),
+        ("density", C.c_double), ("dt", C.c_double),
+        ("workers", C.c_int64), ("gauss_seidel_iters", C.c_int64),
+        ("use_sparse_solver", C.c_int32), ("lock", C.c_int32),
+        ("precision", C.c_int32), ("device", C.c_int32),
+        ("div_tol", C.c_double), ("inner_sweeps", C.c_int64), ("max_refine", C.c_int64),
+    ]
+
+
+class AfStepProfile(C.Structure):
+    _fields_ = [("step_ms", C.c_double), ("sweep_ms", C.c_double), ("rbgs_ms", C.c_double),
+                ("rbgs_launches", C.c_int64), ("kernel_launches", C.c_int64)]
+
+
+class AfFieldDesc(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("off", "nx", "ny", "nz", "sy", "sz", "count")]
+
+
+_E = C.c_void_p
+_ERR = (C.c_char_p, C.c_size_t)
+
+# name -> (restype, argtypes); mirrors include/aeroflux_cuda.h one to one.
+SIGNATURES = {
+    "af_abi_version": (C.c_int, []),
+    "af_config_normalize": (C.c_int, [C.POINTER(AfConfig), *_ERR]),
+    "af_mac_bytes": (C.c_int64, [C.c_int64] * 4),
+    "af_create": (C.c_int, [C.POINTER(AfConfig), C.POINTER(_E), *_ERR]),
+    "af_get_config": (C.c_int, [_E, C.POINTER(AfConfig)]),
+    "af_field_info": (C.c_int, [_E, C.c_int, C.POINTER(AfFieldDesc)]),
+    "af_field_upload": (C.c_int, [_E, C.c_int, C.c_void_p, C.c_size_t]),
+    "af_field_download": (C.c_int, [_E, C.c_int, C.c_void_p, C.c_size_t]),
+    "af_apply_velocity_bc": (C.c_int, [_E]),
+    "af_step": (C.c_int, [_E, C.c_int64]),
+    "af_project": (C.c_int, [_E]),
+    "af_max_divergence": (C.c_int, [_E, C.POINTER(C.c_double)]),
+    "af_kinetic_energy": (C.c_int, [_E, C.POINTER(C.c_double)]),
+    "af_max_velocity": (C.c_int, [_E, C.POINTER(C.c_double)]),
+    "af_cfl": (C.c_int, [_E, C.POINTER(C.c_double)]),
+    "af_enable_sparse_solver": (C.c_int, [_E]),
+    "af_phase_sweep": (C.c_int, [_E, C.c_int, C.c_double]),
+    "af_phase_divergence": (C.c_int, [_E]),
+    "af_phase_red_black": (C.c_int, [_E]),
+    "af_phase_pressure_bc": (C.c_int, [_E]),
+    "af_phase_subtract_gradient": (C.c_int, [_E]),
+    "af_last_projection_stats": (C.c_int, [_E, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "af_profile": (C.c_int, [_E, C.c_int]),
+    "af_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
+    "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "af_seed_taylor_green": (C.c_int, [C.POINTER(AfConfig), C.c_double, C.c_double, C.c_uint64, C.c_uint64,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "af_close": (C.c_int, [_E]),
+    "af_destroy": (None, [_E]),
+    "af_last_error": (C.c_char_p, [_E]),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(af_\w+)\s*\(", text, re.M)))
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the engine library (building it first if it is absent)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build as _build
+            _build.build()
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib

@@ -1,0 +1,632 @@
+// af_fp64.cu -- FP64 plain form of AeroFlux's fractional-step stages for
+// sm_103a.  Every kernel reproduces the reference's binary64 arithmetic bit
+// for bit: explicit round-to-nearest intrinsics (never contracted into FMA,
+// as Go on amd64 never contracts), the reference's left-to-right evaluation
+// order, and sign flips done on the sign bit as Go's unary minus does.
+//
+// The reference runs each stage as a loop nest over Z-slabs with a join
+// between phases; here each stage is one grid-wide kernel and the join is the
+// kernel boundary.  Every stage is per-cell independent, so results do not
+// depend on the launch shape.
+#include "af_internal.h"
+
+#include <math.h>
+
+#include <algorithm>
+
+namespace af {
+namespace {
+
+constexpr unsigned long long kSign = 0x8000000000000000ull;
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double flip(double a) {
+    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(a) ^ kSign));
+}
+
+// Correctly rounded x/6.  Because 6 = 3*2, x/6 is never within ulp/6 of a
+// rounding midpoint, while q + r*c below is within 2^-54 ulp of x/6 (q =
+// RN(x*RN(1/6)), r = x - 6q computed exactly by the FMA, RN(1/6) = (1-2^-54)/6).
+// So RN(q + r*c) = RN(x/6).  This is the multiply-by-reciprocal-plus-remainder
+// division of Markstein (1990) / Brisebarre-Muller-Raina (2004), specialised
+// to divisor 6.  Outside the range where q and r stay normal (and for zero,
+// Inf, NaN) the IEEE division is used.  Three FP64 pipe operations instead of
+// a full reciprocal-refinement sequence.
+__device__ __forceinline__ double div6(double x) {
+    const double c = 0x1.5555555555555p-3;  // RN(1/6)
+    const double ax = fabs(x);
+    if (ax >= 0x1p-960 && ax < 0x1p1020) {
+        const double q = dmul(x, c);
+        const double r = __fma_rn(-6.0, q, x);
+        return __fma_rn(r, c, q);
+    }
+    return x / 6.0;
+}
+
+__device__ __forceinline__ bool gated(const Status* st, int gate) {
+    return st->fault_gate < st->step * 8u + (unsigned)gate;
+}
+
+// ---------------------------------------------------------------------------
+// applyVelocityBC, stencil.go:246-315.
+//
+// The reference writes the wall faces, then reflects tangential ghosts in a
+// fixed order where later passes read ghosts written by earlier ones (edges
+// and corners).  Composed, every written cell equals the sign-flipped value
+// of one interior cell: reflect each ghost coordinate into the interior,
+// flip the sign once per reflection, and read +0 where the source lies on a
+// wall face (zeroed by the first pass).  So one kernel writes each cell once
+// from unwritten cells only, and produces the reference's bits, -0 included.
+// ---------------------------------------------------------------------------
+struct BcComp {
+    double* f;
+    long long s_n, s_1, s_2;  // strides along the normal axis and the two tangential axes
+    int Nn, N1, N2;           // interior extents along those axes
+};
+
+__device__ __forceinline__ double bc_src(const BcComp& c, int G, int n, int a, int b) {
+    if (n == G || n == G + c.Nn) return 0.0;
+    return c.f[(long long)n * c.s_n + (long long)a * c.s_1 + (long long)b * c.s_2];
+}
+
+__global__ void k_velocity_bc(BcComp cu, BcComp cv, BcComp cw, int G, Status* st, int gate) {
+    if (gated(st, gate)) return;
+    const int comp = blockIdx.y / 3, set = blockIdx.y % 3;
+    const BcComp& c = comp == 0 ? cu : (comp == 1 ? cv : cw);
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int n, t1, t2;
+    double val;
+    if (set == 0) {  // wall faces: +0
+        const long long cnt = 2ll * c.N1 * c.N2;
+        if (i >= cnt) return;
+        t1 = G + (int)(i % c.N1);
+        long long r = i / c.N1;
+        t2 = G + (int)(r % c.N2);
+        n = (r / c.N2) ? G + c.Nn : G;
+        val = 0.0;
+    } else if (set == 1) {  // ghosts of the first tangential axis
+        const long long cnt = 2ll * (c.Nn + 1) * c.N2;
+        if (i >= cnt) return;
+        n = G + (int)(i % (c.Nn + 1));
+        long long r = i / (c.Nn + 1);
+        t2 = G + (int)(r % c.N2);
+        const int side = (int)(r / c.N2);
+        t1 = side ? G + c.N1 : G - 1;
+        const int s1 = side ? G + c.N1 - 1 : G;
+        val = flip(bc_src(c, G, n, s1, t2));
+    } else {  // ghosts of the second tangential axis (edges included)
+        const long long cnt = 2ll * (c.Nn + 1) * (c.N1 + 2);
+        if (i >= cnt) return;
+        n = G + (int)(i % (c.Nn + 1));
+        long long r = i / (c.Nn + 1);
+        t1 = G - 1 + (int)(r % (c.N1 + 2));
+        const int side = (int)(r / (c.N1 + 2));
+        t2 = side ? G + c.N2 : G - 1;
+        const int s2 = side ? G + c.N2 - 1 : G;
+        int s1 = t1;
+        bool odd = true;
+        if (t1 == G - 1) { s1 = G; odd = false; }
+        else if (t1 == G + c.N1) { s1 = G + c.N1 - 1; odd = false; }
+        const double s = bc_src(c, G, n, s1, s2);
+        val = odd ? flip(s) : s;
+    }
+    c.f[(long long)n * c.s_n + (long long)t1 * c.s_1 + (long long)t2 * c.s_2] = val;
+}
+
+// ---------------------------------------------------------------------------
+// advectDiffuseAxis / advectComponent / faceVelocity / sampleTrilinear,
+// stencil.go:21-225.
+// ---------------------------------------------------------------------------
+struct SweepArgs {
+    const double* u;
+    const double* v;
+    const double* w;
+    double* tu;
+    double* tv;
+    double* tw;
+    Dims du, dv, dw;
+    int NX, NY, NZ, G;
+    double dt, invH, lam;
+    Status* st;
+    int phase;
+};
+
+// faceVelocity (stencil.go:128-155), only the component on the active axis:
+// the other two feed nothing and have no side effects.
+template <int AX>
+__device__ __forceinline__ double face_vel(const SweepArgs& a, int c, int x, int y, int z) {
+    const double* u = a.u;
+    const double* v = a.v;
+    const double* w = a.w;
+    auto U = [&](int i, int j, int k) { return u[i + j * a.du.sy + k * a.du.sz]; };
+    auto V = [&](int i, int j, int k) { return v[i + j * a.dv.sy + k * a.dv.sz]; };
+    auto W = [&](int i, int j, int k) { return w[i + j * a.dw.sy + k * a.dw.sz]; };
+    if (c == 0) {
+        if (AX == 0) return U(x, y, z);
+        if (AX == 1)
+            return dmul(0.25, dadd(dadd(dadd(V(x - 1, y, z), V(x, y, z)), V(x - 1, y + 1, z)), V(x, y + 1, z)));
+        return dmul(0.25, dadd(dadd(dadd(W(x - 1, y, z), W(x, y, z)), W(x - 1, y, z + 1)), W(x, y, z + 1)));
+    } else if (c == 1) {
+        if (AX == 0)
+            return dmul(0.25, dadd(dadd(dadd(U(x, y - 1, z), U(x + 1, y - 1, z)), U(x, y, z)), U(x + 1, y, z)));
+        if (AX == 1) return V(x, y, z);
+        return dmul(0.25, dadd(dadd(dadd(W(x, y - 1, z), W(x, y, z)), W(x, y - 1, z + 1)), W(x, y, z + 1)));
+    } else {
+        if (AX == 0)
+            return dmul(0.25, dadd(dadd(dadd(U(x, y, z - 1), U(x + 1, y, z - 1)), U(x, y, z)), U(x + 1, y, z)));
+        if (AX == 1)
+            return dmul(0.25, dadd(dadd(dadd(V(x, y, z - 1), V(x, y + 1, z - 1)), V(x, y, z)), V(x, y + 1, z)));
+        return W(x, y, z);
+    }
+}
+
+__device__ __forceinline__ double lerp(double a, double b, double t) {
+    // a*(1-t) + b*t, evaluated as the reference writes it
+    return dadd(dmul(a, dsub(1.0, t)), dmul(b, t));
+}
+
+template <int AX>
+__global__ void k_sweep_fp64(SweepArgs a) {
+    if (gated(a.st, a.phase)) return;
+    const int zr = a.NZ + 1;
+    const int c = blockIdx.z / zr;
+    const int z = a.G + (int)(blockIdx.z % zr);
+    const int x = a.G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = a.G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    // Face-count extents of this component (stencil.go:53-68).
+    const int x1 = a.G + a.NX + (c == 0), y1 = a.G + a.NY + (c == 1), z1 = a.G + a.NZ + (c == 2);
+    if (x >= x1 || y >= y1 || z >= z1) return;
+
+    const Dims& d = c == 0 ? a.du : (c == 1 ? a.dv : a.dw);
+    const double* sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
+    double* dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
+
+    const double vel = face_vel<AX>(a, c, x, y, z);
+    // Backtrace along the active axis only: p -= dt*v*invH.
+    const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+    double pa = dsub((double)ca, dmul(dmul(a.dt, vel), a.invH));
+    const double maxA = (double)(na - 1);
+    if (pa < 0) pa = 0;
+    else if (pa > maxA) pa = maxA;
+
+    // Truncation toward zero as amd64 CVTTSD2SQ does (NaN -> INT64_MIN).  The
+    // two other coordinates are integer faces strictly inside the padded
+    // field, so their floor is the face itself and their weight is +0.
+    long long a0;
+    if (isnan(pa)) a0 = (long long)0x8000000000000000ull;
+    else a0 = (long long)pa;
+    if (a0 >= na - 1) a0 = na - 2;
+    const double ta = dsub(pa, (double)a0);
+    long long x0 = x, y0 = y, z0 = z;
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    if (AX == 0) { x0 = a0; tx = ta; }
+    if (AX == 1) { y0 = a0; ty = ta; }
+    if (AX == 2) { z0 = a0; tz = ta; }
+    // Index arithmetic wraps modulo 2^64, as Go's int does.
+    const unsigned long long i000 =
+        (unsigned long long)x0 + (unsigned long long)y0 * (unsigned long long)d.sy +
+        (unsigned long long)z0 * (unsigned long long)d.sz;
+    if (isnan(pa)) {
+        // Only a NaN coordinate can leave the field; Go bounds-checks the taps
+        // in source order and panics at the first out-of-range one.
+        const unsigned long long sy = d.sy, sz = d.sz, n = d.count;
+        const unsigned long long taps[8] = {i000, i000 + 1, i000 + sy, i000 + sy + 1,
+                                            i000 + sz, i000 + sz + 1, i000 + sz + sy, i000 + sz + sy + 1};
+        bool oob = false;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) oob |= (long long)taps[k] < 0 || taps[k] >= n;
+        if (oob) {
+            atomicMin(&a.st->fault_gate, a.st->step * 8u + (unsigned)a.phase);
+            atomicMin(&a.st->fault_key, fault_key(c, x, y, z));
+            return;  // the faulting face is not written, as the panic leaves it
+        }
+    }
+    const long long sy = d.sy, sz = d.sz;
+    const long long b = (long long)i000;
+    const double c00 = lerp(sd[b], sd[b + 1], tx);
+    const double c10 = lerp(sd[b + sy], sd[b + sy + 1], tx);
+    const double c01 = lerp(sd[b + sz], sd[b + sz + 1], tx);
+    const double c11 = lerp(sd[b + sz + sy], sd[b + sz + sy + 1], tx);
+    const double c0 = lerp(c00, c10, ty);
+    const double c1 = lerp(c01, c11, ty);
+    const double adv = lerp(c0, c1, tz);
+
+    const long long i = (long long)x + (long long)y * sy + (long long)z * sz;
+    double lap = 0.0;
+    if (a.lam != 0) {
+        const long long s = AX == 0 ? 1 : (AX == 1 ? sy : sz);
+        lap = dmul(a.lam, dadd(dsub(sd[i - s], dmul(2.0, sd[i])), sd[i + s]));
+    }
+    dd[i] = dadd(adv, lap);
+}
+
+// ---------------------------------------------------------------------------
+// solvePressureRedBlack's zeroing (project.go:81-83) fused with
+// computeDivergence (project.go:42-62).  Also stores B = h2*Div, the product
+// every red-black update recomputes (project.go:126), so the sweeps read it
+// instead of multiplying again: same bits, one FP64 multiply fewer per update.
+// ---------------------------------------------------------------------------
+__global__ void k_divergence_fp64(Geom g, const double* __restrict__ u, const double* __restrict__ v,
+                                  const double* __restrict__ w, double* __restrict__ p, double* __restrict__ dv,
+                                  double* __restrict__ bb, double scale, double h2, int zero_p, Status* st,
+                                  int gate) {
+    if (gated(st, gate)) return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= g.p.nx || y >= g.p.ny) return;
+    const long long i = x + y * g.p.sy + z * g.p.sz;
+    if (zero_p) p[i] = 0.0;
+    const int G = g.G;
+    if (x < G || x >= G + g.NX || y < G || y >= G + g.NY || z < G || z >= G + g.NZ) return;
+    const long long iu = x + y * g.u.sy + z * g.u.sz;
+    const long long iv = x + y * g.v.sy + z * g.v.sz;
+    const long long iw = x + y * g.w.sy + z * g.w.sz;
+    const double du = dsub(u[iu + 1], u[iu]);
+    const double dvv = dsub(v[iv + g.v.sy], v[iv]);
+    const double dw = dsub(w[iw + g.w.sz], w[iw]);
+    const double d = dmul(scale, dadd(dadd(du, dvv), dw));
+    dv[i] = d;
+    bb[i] = dmul(h2, d);
+}
+
+// ---------------------------------------------------------------------------
+// gaussSeidelSweep, project.go:103-130, with applyPressureBC folded in.
+// Before each colour the reference mirrors the interior into the ghosts
+// (project.go:89,93); a face ghost of a cell being updated then holds that
+// cell's own pre-update value, so the sweep reads the centre instead and the
+// ghosts are materialised once, after the last sweep (k_pressure_bc).
+// ---------------------------------------------------------------------------
+__global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __restrict__ bb, int color, Status* st,
+                            int gate) {
+    if (gated(st, gate)) return;
+    const int G = g.G;
+    const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int z = G + (int)blockIdx.z;
+    if (y >= G + g.NY) return;
+    const int start = (((G + y + z) & 1) != color) ? G + 1 : G;
+    const int x = start + 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (x >= G + g.NX) return;
+    const long long sy = g.p.sy, sz = g.p.sz;
+    const long long i = x + y * sy + z * sz;
+    const double pc = p[i];
+    const double xm = x > G ? p[i - 1] : pc;
+    const double xp = x < G + g.NX - 1 ? p[i + 1] : pc;
+    const double ym = y > G ? p[i - sy] : pc;
+    const double yp = y < G + g.NY - 1 ? p[i + sy] : pc;
+    const double zm = z > G ? p[i - sz] : pc;
+    const double zp = z < G + g.NZ - 1 ? p[i + sz] : pc;
+    const double sum = dadd(dadd(dadd(dadd(dadd(xm, xp), ym), yp), zm), zp);
+    p[i] = div6(dsub(sum, bb[i]));
+}
+
+// applyPressureBC, project.go:139-163: composed, every ghost of the first
+// layer holds the interior cell at the clamped coordinates.
+__global__ void k_pressure_bc(Geom g, double* __restrict__ p, Status* st, int gate) {
+    if (gated(st, gate)) return;
+    const int G = g.G, NX = g.NX, NY = g.NY, NZ = g.NZ;
+    const int set = blockIdx.y;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int x, y, z;
+    if (set == 0) {
+        if (i >= 2ll * NY * NZ) return;
+        y = G + (int)(i % NY);
+        long long r = i / NY;
+        z = G + (int)(r % NZ);
+        x = (r / NZ) ? G + NX : G - 1;
+    } else if (set == 1) {
+        if (i >= 2ll * (NX + 2) * NZ) return;
+        x = G - 1 + (int)(i % (NX + 2));
+        long long r = i / (NX + 2);
+        z = G + (int)(r % NZ);
+        y = (r / NZ) ? G + NY : G - 1;
+    } else {
+        if (i >= 2ll * (NX + 2) * (NY + 2)) return;
+        x = G - 1 + (int)(i % (NX + 2));
+        long long r = i / (NX + 2);
+        y = G - 1 + (int)(r % (NY + 2));
+        z = (r / (NY + 2)) ? G + NZ : G - 1;
+    }
+    const int cx = min(max(x, G), G + NX - 1);
+    const int cy = min(max(y, G), G + NY - 1);
+    const int cz = min(max(z, G), G + NZ - 1);
+    p[x + y * g.p.sy + z * g.p.sz] = p[cx + cy * g.p.sy + cz * g.p.sz];
+}
+
+// subtractGradient, project.go:172-205.
+__global__ void k_gradient_fp64(Geom g, const double* __restrict__ p, double* __restrict__ u, double* __restrict__ v,
+                                double* __restrict__ w, double scale, Status* st, int gate) {
+    if (gated(st, gate)) return;
+    const int G = g.G;
+    const int zr = g.NZ + 1;
+    const int c = blockIdx.z / zr;
+    const int z = G + (int)(blockIdx.z % zr);
+    const int x = G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int x1 = G + g.NX + (c == 0), y1 = G + g.NY + (c == 1), z1 = G + g.NZ + (c == 2);
+    if (x >= x1 || y >= y1 || z >= z1) return;
+    const long long ip = x + y * g.p.sy + z * g.p.sz;
+    if (c == 0) {
+        const long long i = x + y * g.u.sy + z * g.u.sz;
+        u[i] = dsub(u[i], dmul(scale, dsub(p[ip], p[ip - 1])));
+    } else if (c == 1) {
+        const long long i = x + y * g.v.sy + z * g.v.sz;
+        v[i] = dsub(v[i], dmul(scale, dsub(p[ip], p[ip - g.p.sy])));
+    } else {
+        const long long i = x + y * g.w.sy + z * g.w.sz;
+        w[i] = dsub(w[i], dmul(scale, dsub(p[ip], p[ip - g.p.sz])));
+    }
+}
+
+__global__ void k_step_tick(Status* st) { st->step += 1; }
+
+// B = h2*Div over the interior, for the red-black phase hook when Div was
+// supplied directly instead of by the divergence kernel.
+__global__ void k_b_from_div(Geom g, const double* __restrict__ dv, double* __restrict__ bb, double h2) {
+    const int G = g.G;
+    const int x = G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int z = G + (int)blockIdx.z;
+    if (x >= G + g.NX || y >= G + g.NY) return;
+    const long long i = x + y * g.p.sy + z * g.p.sz;
+    bb[i] = dmul(h2, dv[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics.  A max is exact in any order; NaN is skipped as the
+// reference's `if a > mx` skips it.  Non-negative doubles order like their
+// bit patterns, so one atomicMax per block combines the blocks.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long abs_bits(double d) {
+    const double a = fabs(d);
+    return isnan(a) ? 0ull : (unsigned long long)__double_as_longlong(a);
+}
+
+__device__ __forceinline__ void block_max_commit(unsigned long long m, unsigned long long* out) {
+    __shared__ unsigned long long sm[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    if ((tid & 31) == 0) sm[tid >> 5] = m;
+    __syncthreads();
+    if (tid < 32) {
+        m = tid < (nthreads + 31) / 32 ? sm[tid] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+            m = t > m ? t : m;
+        }
+        if (tid == 0 && m) atomicMax(out, m);
+    }
+}
+
+// MaxDivergence, project.go:210-232.
+__global__ void k_max_divergence(Geom g, const double* __restrict__ u, const double* __restrict__ v,
+                                 const double* __restrict__ w, double invH, unsigned long long* out) {
+    const int G = g.G;
+    const int x = G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = G + (int)blockIdx.y;
+    const int z = G + (int)blockIdx.z;
+    unsigned long long m = 0;
+    if (x < G + g.NX) {
+        const long long iu = x + y * g.u.sy + z * g.u.sz;
+        const long long iv = x + y * g.v.sy + z * g.v.sz;
+        const long long iw = x + y * g.w.sy + z * g.w.sz;
+        const double d = dmul(invH, dadd(dadd(dsub(u[iu + 1], u[iu]), dsub(v[iv + g.v.sy], v[iv])),
+                                         dsub(w[iw + g.w.sz], w[iw])));
+        m = abs_bits(d);
+    }
+    block_max_commit(m, out);
+}
+
+// MaxVelocity, stencil.go:319-331: every element of U, V, W, ghosts included.
+__global__ void k_max_abs3(const double* __restrict__ u, long long nu, const double* __restrict__ v, long long nv,
+                           const double* __restrict__ w, long long nw, unsigned long long* out) {
+    unsigned long long m = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += stride) {
+        const unsigned long long t = abs_bits(u[i]);
+        m = t > m ? t : m;
+    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+        const unsigned long long t = abs_bits(v[i]);
+        m = t > m ? t : m;
+    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += stride) {
+        const unsigned long long t = abs_bits(w[i]);
+        m = t > m ? t : m;
+    }
+    block_max_commit(m, out);
+}
+
+// KineticEnergy, project.go:238-258.  The reference sums serially; this sums
+// each z-plane in a fixed per-thread order and a fixed shuffle tree, then the
+// planes in a fixed tree, so the result depends on the grid only and is
+// bit-identical run to run (it differs from the serial sum by rounding).
+constexpr int kKeThreads = 256;
+
+__device__ __forceinline__ double block_sum_fixed(double s) {
+    __shared__ double sm[kKeThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = dadd(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    s = threadIdx.x < kKeThreads / 32 ? sm[threadIdx.x] : 0.0;
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = dadd(s, __shfl_xor_sync(0xffffffffu, s, o));
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(kKeThreads) k_ke_planes(Geom g, const double* __restrict__ u,
+                                                          const double* __restrict__ v,
+                                                          const double* __restrict__ w, double* partials) {
+    const int G = g.G;
+    const int z = G + (int)blockIdx.x;
+    const long long n = (long long)g.NX * g.NY;
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < n; k += kKeThreads) {
+        const int x = G + (int)(k % g.NX), y = G + (int)(k / g.NX);
+        const long long iu = x + y * g.u.sy + z * g.u.sz;
+        const long long iv = x + y * g.v.sy + z * g.v.sz;
+        const long long iw = x + y * g.w.sy + z * g.w.sz;
+        const double uc = dmul(0.5, dadd(u[iu], u[iu + 1]));
+        const double vc = dmul(0.5, dadd(v[iv], v[iv + g.v.sy]));
+        const double wc = dmul(0.5, dadd(w[iw], w[iw + g.w.sz]));
+        s = dadd(s, dadd(dadd(dmul(uc, uc), dmul(vc, vc)), dmul(wc, wc)));
+    }
+    s = block_sum_fixed(s);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kKeThreads) k_ke_final(const double* partials, int n, double* out) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n; k += kKeThreads) s = dadd(s, partials[k]);
+    s = block_sum_fixed(s);
+    if (threadIdx.x == 0) *out = s;
+}
+
+inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// Eight independent DFMA chains per thread: issue-rate bound, not latency bound.
+constexpr int kRateIters = 2048, kRateChains = 8;
+__global__ void k_fp64_rate(double* out, double seed) {
+    double a[kRateChains];
+#pragma unroll
+    for (int c = 0; c < kRateChains; ++c) a[c] = seed + threadIdx.x + c;
+    const double m = 0.999999999, k = 1e-9;
+    for (int i = 0; i < kRateIters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kRateChains; ++c) a[c] = __fma_rn(a[c], m, k);
+    }
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < kRateChains; ++c) s += a[c];
+    if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+bool measure_fp64_rate(double* fma_per_s) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+    double* out = nullptr;
+    if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return false;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 8, threads = 256;
+    k_fp64_rate<<<blocks, threads>>>(out, 1.0);  // warm-up
+    cudaEventRecord(a);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) k_fp64_rate<<<blocks, threads>>>(out, 1.0 + r);
+    cudaEventRecord(b);
+    bool ok = cudaEventSynchronize(b) == cudaSuccess;
+    float ms = 0;
+    ok = ok && cudaEventElapsedTime(&ms, a, b) == cudaSuccess;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (!ok || ms <= 0) return false;
+    *fma_per_s = (double)blocks * threads * kRateIters * kRateChains * reps / (ms * 1e-3);
+    return true;
+}
+
+namespace {
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_velocity_bc(const Geom& g, double* u, double* v, double* w, Status* st, int gate, cudaStream_t s) {
+    BcComp cu{u, 1, g.u.sy, g.u.sz, g.NX, g.NY, g.NZ};
+    BcComp cv{v, g.v.sy, 1, g.v.sz, g.NY, g.NX, g.NZ};
+    BcComp cw{w, g.w.sz, 1, g.w.sy, g.NZ, g.NX, g.NY};
+    long long mx = 0;
+    for (const BcComp* c : {&cu, &cv, &cw}) {
+        mx = std::max(mx, 2ll * c->N1 * c->N2);
+        mx = std::max(mx, 2ll * (c->Nn + 1) * c->N2);
+        mx = std::max(mx, 2ll * (c->Nn + 1) * (c->N1 + 2));
+    }
+    dim3 grid(cdiv(mx, 256), 9);
+    k_velocity_bc<<<grid, 256, 0, s>>>(cu, cv, cw, g.G, st, gate);
+}
+
+void launch_sweep_fp64(const Geom& g, int axis, const Fields& f, double dt, double invH, double lam, Status* st,
+                       int phase, cudaStream_t s) {
+    SweepArgs a;
+    a.u = f.u; a.v = f.v; a.w = f.w;
+    a.tu = f.t0; a.tv = f.t1; a.tw = f.t2;
+    a.du = g.u; a.dv = g.v; a.dw = g.w;
+    a.NX = g.NX; a.NY = g.NY; a.NZ = g.NZ; a.G = g.G;
+    a.dt = dt; a.invH = invH; a.lam = lam;
+    a.st = st; a.phase = phase;
+    dim3 block(64, 4);
+    dim3 grid(cdiv(g.NX + 1, 64), cdiv(g.NY + 1, 4), 3 * (g.NZ + 1));
+    if (axis == 0) k_sweep_fp64<0><<<grid, block, 0, s>>>(a);
+    else if (axis == 1) k_sweep_fp64<1><<<grid, block, 0, s>>>(a);
+    else k_sweep_fp64<2><<<grid, block, 0, s>>>(a);
+}
+
+void launch_divergence_fp64(const Geom& g, const Fields& f, double* b, double scale, double h2, bool zero_p,
+                            Status* st, int gate, cudaStream_t s) {
+    dim3 block(64, 4);
+    dim3 grid(cdiv(g.p.nx, 64), cdiv(g.p.ny, 4), g.p.nz);
+    k_divergence_fp64<<<grid, block, 0, s>>>(g, f.u, f.v, f.w, f.p, f.div, b, scale, h2, zero_p ? 1 : 0, st, gate);
+}
+
+void launch_rbgs_fp64(const Geom& g, double* p, const double* b, int color, Status* st, int gate, cudaStream_t s) {
+    dim3 block(32, 4);
+    dim3 grid(cdiv((g.NX + 1) / 2, 32), cdiv(g.NY, 4), g.NZ);
+    k_rbgs_fp64<<<grid, block, 0, s>>>(g, p, b, color, st, gate);
+}
+
+void launch_pressure_bc_fp64(const Geom& g, double* p, Status* st, int gate, cudaStream_t s) {
+    long long mx = std::max(2ll * g.NY * g.NZ, std::max(2ll * (g.NX + 2) * g.NZ, 2ll * (g.NX + 2) * (g.NY + 2)));
+    dim3 grid(cdiv(mx, 256), 3);
+    k_pressure_bc<<<grid, 256, 0, s>>>(g, p, st, gate);
+}
+
+void launch_gradient_fp64(const Geom& g, const Fields& f, double scale, Status* st, int gate, cudaStream_t s) {
+    dim3 block(64, 4);
+    dim3 grid(cdiv(g.NX + 1, 64), cdiv(g.NY + 1, 4), 3 * (g.NZ + 1));
+    k_gradient_fp64<<<grid, block, 0, s>>>(g, f.p, f.u, f.v, f.w, scale, st, gate);
+}
+
+void launch_step_tick(Status* st, cudaStream_t s) { k_step_tick<<<1, 1, 0, s>>>(st); }
+
+void launch_b_from_div(const Geom& g, const double* div, double* b, double h2, cudaStream_t s) {
+    dim3 block(64, 4);
+    dim3 grid(cdiv(g.NX, 64), cdiv(g.NY, 4), g.NZ);
+    k_b_from_div<<<grid, block, 0, s>>>(g, div, b, h2);
+}
+
+void launch_max_divergence(const Geom& g, const double* u, const double* v, const double* w, double invH,
+                           unsigned long long* out, cudaStream_t s) {
+    dim3 grid(cdiv(g.NX, 128), g.NY, g.NZ);
+    k_max_divergence<<<grid, 128, 0, s>>>(g, u, v, w, invH, out);
+}
+
+void launch_max_abs3(const double* u, long long nu, const double* v, long long nv, const double* w, long long nw,
+                     unsigned long long* out, cudaStream_t s) {
+    long long n = std::max(nu, std::max(nv, nw));
+    unsigned blocks = (unsigned)std::min<long long>(cdiv(n, 256), 152 * 8);
+    k_max_abs3<<<blocks, 256, 0, s>>>(u, nu, v, nv, w, nw, out);
+}
+
+void launch_kinetic_energy(const Geom& g, const double* u, const double* v, const double* w, double* partials,
+                           double* out, cudaStream_t s) {
+    k_ke_planes<<<g.NZ, kKeThreads, 0, s>>>(g, u, v, w, partials);
+    k_ke_final<<<1, kKeThreads, 0, s>>>(partials, g.NZ, out);
+}
+
+}  // namespace af

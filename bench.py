@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the fractional-step Step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step" = one Step of the engine): a single 256^3 MAC grid in
+binary64, H=1/256, DT=0.001, Viscosity=1e-5, 200 red-black sweep pairs per
+projection, Taylor-Green vortex (amplitude 1) plus seeded uniform +-0.01
+PCG32 noise.  Metric: interior cell-steps per second (NX*NY*NZ*steps/s, the
+reference's Mcell/s of bench_test.go:32).
+
+ours: `value` is device time (CUDA event nodes carried by the step graph on
+the engine's stream) over exactly K steps with the field resident in HBM; the
+working set (1.1 GB per grid) is far larger than L2.  `e2e` times the same
+step through the C ABI with the field uploaded from pinned host memory and
+the step's result (MaxDivergence) read back, every step.  `roofline` is the
+red-black sweep kernel, the dominant one.  `cpu_baseline` times the CPU
+oracle (a C restatement of the reference's Go CPU path) on a bounded sample.
+
+reference: the reference's CPU algorithm (the oracle, since Go is not
+available) on all host cores, W + K steps of the same workload.
+
+N > 1 runs independent replicas (the path has no exchange step): one grid per
+GPU, no collective on the data path; the barrier and max-over-ranks timing
+use a gloo process group.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s at 256^3 (FP64 vs mixed, same div tol); served p50/p99 latency"
+UNIT = "cell-steps/s"
+N = 256
+DT = 0.001
+NU = 1e-5
+GSI = 200
+NOISE = 0.01
+WORKLOAD = f"plain-fp64 {N}^3 MAC grid, H=1/{N}, DT={DT}, Viscosity={NU}, {GSI} red-black pairs/projection"
+HBM_FALLBACK_GBS = 6800.0
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+class Dist:
+    """Barrier / max-reduce across replica ranks (gloo; nothing on the data path)."""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.d = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.d.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.d.all_reduce(t, op=self.d.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.d.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        self.f.close()
+        os.unlink(self.f.name)
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        ids = {r[0] for r in rows}
+        if len(ids) > 1:
+            rows = [r for r in rows if r[0] == str(self.idx)]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def profiled_traffic(name: str) -> float | None:
+    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.md,
+    line `dram_bytes_per_launch: <int>`), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def base_config():
+    from aeroflux_gb300.workloads import PLAIN_256
+    return PLAIN_256
+
+
+def run_oracle_steps(warmup: int, steps: int, threads: int):
+    """The CPU path (oracle) on the same workload: seconds per step."""
+    from aeroflux_gb300 import Config
+    from aeroflux_gb300.workloads import taylor_green
+    from oracle.oracle import OracleEngine
+    cfg = Config(NX=N, NY=N, NZ=N, H=1.0 / N, DT=DT, Viscosity=NU, Density=1.0, GaussSeidelIters=GSI)
+    u, v, w = taylor_green(cfg, 1.0, NOISE, 42, 0)
+    with OracleEngine(nx=N, ny=N, nz=N, h=1.0 / N, dt=DT, viscosity=NU, density=1.0,
+                      gauss_seidel_iters=GSI, workers=threads) as o:
+        o.data(1)[:] = u
+        o.data(2)[:] = v
+        o.data(3)[:] = w
+        o.apply_velocity_bc()
+        for _ in range(warmup):
+            o.step()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step()
+        return (time.perf_counter() - t0) / max(steps, 1)
+
+
+def common_fields(args, world):
+    return {
+        "metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: Taylor-Green vortex amplitude 1 + uniform +-0.01 PCG32 noise (seed 42, stream=rank)",
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "dt": DT, "viscosity": NU, "gauss_seidel_iters": GSI,
+                   "precision": "fp64 (bit-identical to the CPU path)",
+                   "l2": "inputs larger than L2: 1.10 GB arena per grid vs 129 MB L2",
+                   "parallelism": f"replicas x{world} (one grid per GPU, no collective)"},
+    }
+
+
+def bench_reference(args):
+    rank, _, world = rank_info()
+    if rank != 0:
+        return 0
+    threads = cpu_threads()
+    sec = run_oracle_steps(args.warmup, args.steps, threads)
+    val = N ** 3 / sec
+    line = common_fields(args, world)
+    line.update({
+        "impl": "reference", "value": val, "ms_per_step": sec * 1e3,
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.warmup} warm-up + {args.steps} timed Steps of the {N}^3 workload, "
+                                   f"C restatement of the Go CPU path, {threads} worker threads"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def bench_ours(args):
+    import numpy as np
+
+    from aeroflux_gb300 import _lib as L
+    from aeroflux_gb300 import New
+    from aeroflux_gb300.workloads import taylor_green
+
+    rank, local, world = rank_info()
+    dist = Dist(world)
+    wl = base_config()
+    cfg = wl.config(Device=local)
+    e = New(cfg)
+    u, v, w = taylor_green(e.Cfg, 1.0, NOISE, 42, rank)
+    for name, a in (("U", u), ("V", v), ("W", w)):
+        e.upload(name, a)
+    e.applyVelocityBC()
+    e.Profile(True)
+    for _ in range(args.warmup):
+        e.Step(1)
+
+    # --- device-timed region: exactly K steps --------------------------------
+    clocks = ClockSampler(local)
+    dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    dev_ms = rb_ms = sw_ms = 0.0
+    t0 = time.perf_counter()
+    prof = None
+    for _ in range(args.steps):
+        e.Step(1)  # synchronous: returns after the step graph completes
+        prof = e.LastStepProfile()
+        dev_ms += prof.step_ms
+        rb_ms += prof.rbgs_ms
+        sw_ms += prof.sweep_ms
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dist.barrier()
+    dev_s = dist.max(dev_ms / 1e3)
+    cells = N ** 3
+    value = cells * args.steps * world / dev_s
+    launches = prof.kernel_launches * args.steps
+    rb_launch_s = rb_ms / 1e3 / (prof.rbgs_launches * args.steps)
+    sweep_ms_per = sw_ms / (6 * args.steps)
+    md = e.MaxDivergence()
+
+    # --- end to end through the C ABI with host buffers ---------------------
+    e.Profile(False)
+    try:
+        import torch
+        pin = torch.cuda.is_available()
+    except ImportError:
+        pin = False
+    host = []
+    for a in (u, v, w):
+        if pin:
+            t = torch.from_numpy(a).pin_memory()
+            host.append((t, t.data_ptr(), a.size))
+        else:
+            host.append((a, a.ctypes.data, a.size))
+    lib = L.lib()
+    out = C.c_double()
+    e2e_steps = max(3, args.steps // 2)
+
+    def e2e_step():
+        for fid, (_, ptr, n) in zip((1, 2, 3), host):
+            e._check(lib.af_field_upload(e._h, fid, ptr, n))
+        e._check(lib.af_step(e._h, 1))
+        e._check(lib.af_max_divergence(e._h, C.byref(out)))
+
+    e2e_step()  # warm-up (graph rebuild without event nodes)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_val = cells * e2e_steps * world / e2e_s
+    h2d = 8 * (u.size + v.size + w.size)
+
+    # --- roofline of the dominant kernel (one red-black colour sweep) --------
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 1.5 * 8 * cells  # 3b per cell per red+black pair, half per colour launch
+    achieved = alg_bytes / rb_launch_s / 1e9
+    traffic = profiled_traffic("rbgs_fp64_256")
+    fma_rate = C.c_double()
+    lib.af_device_fp64_rate(local, C.byref(fma_rate))
+    fp64_inst = 9 * cells / 2  # per update: 5 adds, 1 sub, and mul+2 FMA for the exact /6
+    fp64_ach = fp64_inst / rb_launch_s
+
+    dist.close()
+    if rank != 0:
+        return 0
+    line = common_fields(args, world)
+    line.update({
+        "value": value, "ms_per_step": dev_s * 1e3 / args.steps, "wall_ms_per_step": wall * 1e3 / args.steps,
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8,
+                "steps": e2e_steps, "host_memory": "pinned" if pin else "pageable"},
+        "roofline": {"bound": "hbm", "kernel": "k_rbgs_fp64 (one colour sweep)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": traffic, "launch_us": rb_launch_s * 1e6,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "fp64_pipe": {"achieved": fp64_ach, "peak": fma_rate.value, "unit": "FP64 inst/s",
+                                   "frac": fp64_ach / fma_rate.value if fma_rate.value else None,
+                                   "inst_per_update": 9}},
+        "stages_ms_per_step": {"rbgs": rb_ms / args.steps, "sweeps": sw_ms / args.steps,
+                               "sweep_each": sweep_ms_per, "step": dev_s * 1e3 / args.steps},
+        "max_divergence_after": md,
+        "clocks": clk,
+    })
+    if world == 1 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        sec = run_oracle_steps(0, 1, threads)
+        line["cpu_baseline"] = {"value": cells / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 Step of the {N}^3 workload on the CPU oracle (C restatement of "
+                                          f"the Go path), {threads} worker threads, {sec:.1f} s"}
+    print(json.dumps(line), flush=True)
+    e.Close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

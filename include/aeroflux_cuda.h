@@ -1,0 +1,213 @@
+/*
+ * aeroflux_cuda.h -- C ABI of libaeroflux_cuda, the GB300 (sm_103a) engine for
+ * AeroFlux's fractional-step timestep: semi-Lagrangian advection, axis-swept
+ * explicit diffusion and red-black Gauss-Seidel pressure projection.
+ *
+ * The ABI is what a cgo shim binds to keep the Go API of the reference
+ * package `aeroflux` (module AeroFlex) as a drop-in:
+ *
+ *   aeroflux.New(cfg)      -> af_create            (aeroflux.go:176-213)
+ *   (*Engine).Step()       -> af_step(e, 1)        (aeroflux.go:348-409)
+ *   (*Engine).MaxDivergence-> af_max_divergence    (project.go:210-232)
+ *   (*Engine).Close()      -> af_close/af_destroy  (aeroflux.go:419-439)
+ *   Mesh.Data(&f) views    -> af_field_download / af_field_upload in the
+ *                             padded MAC layout of grid.go:79-134
+ *
+ * Conventions
+ *   - Every function returns AF_OK (0) or a negative af_status.  No C++
+ *     exception crosses the ABI.  af_last_error(e) returns the message of the
+ *     engine's last failure; af_create reports into the caller's buffer.
+ *   - Messages reproduce the reference's Go error text, "aeroflux: ..." prefix
+ *     included.
+ *   - The engine owns all device memory.  Fields live in one device
+ *     allocation laid out exactly like the reference's arena (grid.go:101-134:
+ *     P, U, V, W, Div, Tmp0, Tmp1, Tmp2, each rounded up to 128 bytes, x unit
+ *     stride, SY = padded nx, SZ = padded nx*ny).
+ *   - One engine is driven by one host thread at a time; it owns one CUDA
+ *     stream.  Calls are synchronous: they return once the device work they
+ *     enqueue has finished.  Results are bit-identical run to run.
+ */
+#ifndef AEROFLUX_CUDA_H
+#define AEROFLUX_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AF_ABI_VERSION 1
+
+typedef enum af_status {
+    AF_OK = 0,
+    AF_ERR_CONFIG = -1,      /* Normalize rejected the configuration */
+    AF_ERR_CUDA = -2,        /* CUDA runtime failure or no usable device */
+    AF_ERR_FAULT = -3,       /* contained fault: the device-side analogue of the
+                                reference's guard-page fault (a NaN backtrace
+                                coordinate driving an index out of range) */
+    AF_ERR_ARG = -4,         /* bad argument: NULL, unknown field, wrong count */
+    AF_ERR_UNSUPPORTED = -5, /* feature not available (the Darwin direct solver) */
+    AF_ERR_CLOSED = -6,      /* engine already closed */
+    AF_ERR_NOMEM = -7        /* device or host allocation failed */
+} af_status;
+
+/* Arithmetic form of the step.  AF_PRECISION_FP64 is the reference's
+ * algorithm in binary64 with bit-identical results; AF_PRECISION_MIXED runs
+ * advection, diffusion and the inner pressure sweeps in binary32 inside
+ * binary64 iterative refinement. */
+typedef enum af_precision {
+    AF_PRECISION_FP64 = 0,
+    AF_PRECISION_MIXED = 1
+} af_precision;
+
+/* Config, aeroflux.go:14-41.  Go ints are 64-bit.  Fields after `lock` are
+ * GB300 extensions; zero selects the reference's behaviour. */
+typedef struct af_config {
+    int64_t nx, ny, nz;          /* interior cell counts */
+    int64_t ghost;               /* halo thickness, default 1 */
+    double h;                    /* cell size, default 1/max(nx,ny,nz) */
+    double viscosity;            /* kinematic viscosity nu */
+    double density;              /* rho, default 1 */
+    double dt;                   /* fixed timestep, default from Normalize */
+    int64_t workers;             /* accepted and normalized like the reference;
+                                    results never depend on it */
+    int64_t gauss_seidel_iters;  /* red-black sweep pairs per projection, default 24 */
+    int32_t use_sparse_solver;   /* the Darwin direct solver: never available */
+    int32_t lock;                /* residency request: device memory is always resident */
+    /* --- extensions --- */
+    int32_t precision;           /* af_precision */
+    int32_t device;              /* CUDA device ordinal the engine lives on */
+    double div_tol;              /* MIXED: stop refining once max|div| <= div_tol (0: 1e-10) */
+    int64_t inner_sweeps;        /* MIXED: binary32 smoothing sweeps per level (0: default) */
+    int64_t max_refine;          /* MIXED: cap on refinement passes per projection (0: 30) */
+} af_config;
+
+/* Field, grid.go:12-21.  off is the byte offset inside the engine arena. */
+typedef struct af_field_desc {
+    int64_t off, nx, ny, nz, sy, sz, count;
+} af_field_desc;
+
+/* Field ids in arena order, grid.go:60-67. */
+typedef enum af_field {
+    AF_FIELD_P = 0,
+    AF_FIELD_U = 1,
+    AF_FIELD_V = 2,
+    AF_FIELD_W = 3,
+    AF_FIELD_DIV = 4,
+    AF_FIELD_TMP0 = 5,
+    AF_FIELD_TMP1 = 6,
+    AF_FIELD_TMP2 = 7
+} af_field;
+
+typedef struct af_engine af_engine;
+
+/* Library ABI version (AF_ABI_VERSION of the build). */
+int af_abi_version(void);
+
+/* (*Config).Normalize, aeroflux.go:47-113: fills defaults in place and
+ * validates.  On rejection returns AF_ERR_CONFIG and writes the reference's
+ * message into err (if non-NULL). */
+int af_config_normalize(af_config* cfg, char* err, size_t errlen);
+
+/* MACBytes, grid.go:138-144: arena footprint in bytes, 0 for invalid extents. */
+int64_t af_mac_bytes(int64_t nx, int64_t ny, int64_t nz, int64_t ghost);
+
+/* New, aeroflux.go:176-213: normalize, allocate the device arena, zero every
+ * field (grid.go:158-163).  *out is NULL on failure and err holds the text. */
+int af_create(const af_config* cfg, af_engine** out, char* err, size_t errlen);
+
+/* Engine.Cfg after Normalize. */
+int af_get_config(const af_engine* e, af_config* out);
+
+/* Current descriptor of a field.  Descriptors swap during a step
+ * (commitVelocity, stencil.go:230-235) and return to their slots after every
+ * complete step. */
+int af_field_info(const af_engine* e, int field, af_field_desc* out);
+
+/* Mesh.Data(&f) (grid.go:147-149) as explicit copies of the whole padded
+ * field: count must equal the descriptor's count. */
+int af_field_upload(af_engine* e, int field, const double* host, size_t count);
+int af_field_download(af_engine* e, int field, double* host, size_t count);
+
+/* applyVelocityBC, stencil.go:246-315 (callers seed, then apply the BC). */
+int af_apply_velocity_bc(af_engine* e);
+
+/* Step, aeroflux.go:348-409, nsteps times.  Stops at the first step that
+ * contains a fault and returns AF_ERR_FAULT with the reference's message
+ * ("aeroflux: guard-page fault contained: runtime error: ..."); the state is
+ * then partly advanced, as in the reference. */
+int af_step(af_engine* e, int64_t nsteps);
+
+/* project, project.go:12-34 (the reference's tests call it directly). */
+int af_project(af_engine* e);
+
+/* Diagnostics: MaxDivergence (project.go:210-232, exact), KineticEnergy
+ * (project.go:238-258, fixed-order tree sum), MaxVelocity and CFL
+ * (stencil.go:319-338, exact). */
+int af_max_divergence(af_engine* e, double* out);
+int af_kinetic_energy(af_engine* e, double* out);
+int af_max_velocity(af_engine* e, double* out);
+int af_cfl(af_engine* e, double* out);
+
+/* EnableSparseSolver (sparse_fallback.go:17-19 on non-Darwin): always
+ * AF_ERR_UNSUPPORTED with the reference's fallback message. */
+int af_enable_sparse_solver(af_engine* e);
+
+/* Phase hooks, one reference phase each, for stage-level parity tests:
+ * dispatch(sweepFn)+commitVelocity for one axis (0=x,1=y,2=z) at dt
+ * (stencil.go:21-25,230-235), computeDivergence (project.go:42-62),
+ * solvePressureRedBlack (project.go:73-100), applyPressureBC
+ * (project.go:139-163), subtractGradient (project.go:172-205). */
+int af_phase_sweep(af_engine* e, int axis, double dt);
+int af_phase_divergence(af_engine* e);
+int af_phase_red_black(af_engine* e);
+int af_phase_pressure_bc(af_engine* e);
+int af_phase_subtract_gradient(af_engine* e);
+
+/* Statistics of the last projection of a MIXED engine: refinement passes
+ * and the FP64 max|div| reached.  FP64 engines report 0 passes. */
+int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div);
+
+/* Device-time profile of the last Step, from event nodes the step graph
+ * carries while profiling is on (af_profile).  No counterpart in the
+ * reference, which reports only wall-clock Mcell/s (bench_test.go:26-32). */
+typedef struct af_step_profile {
+    double step_ms;           /* whole step */
+    double sweep_ms;          /* the six advection/diffusion sweeps (BC passes excluded) */
+    double rbgs_ms;           /* the red-black sweeps of both projections */
+    int64_t rbgs_launches;    /* red-black kernel launches per step */
+    int64_t kernel_launches;  /* kernel launches per step */
+} af_step_profile;
+
+/* Turns event-node profiling of the step graph on or off (rebuilds it). */
+int af_profile(af_engine* e, int enable);
+int af_last_step_profile(af_engine* e, af_step_profile* out);
+
+/* Measures the device's binary64 FMA issue rate (independent DFMA chains),
+ * in FMA instructions per second, for the FP64 roofline. */
+int af_device_fp64_rate(int device, double* fma_per_s);
+
+/* Synthetic input (no counterpart in the reference API; its tests seed a
+ * trigonometric field straight into arena views, engine_test.go:302-335).
+ * Fills host arrays u, v, w -- the padded counts of U, V, W for the
+ * normalized cfg -- with a Taylor-Green vortex of amplitude amp sampled at the
+ * staggered faces plus i.i.d. uniform [-noise, noise] from PCG32 (initstate
+ * seed, stream `stream`), over seedVortex's index ranges and in its field and
+ * loop order; every other element is zero.  Apply the velocity BC after
+ * uploading. */
+int af_seed_taylor_green(const af_config* cfg, double amp, double noise, uint64_t seed, uint64_t stream,
+                         double* u, double* v, double* w);
+
+/* Close, aeroflux.go:419-439: release device memory.  Idempotent. */
+int af_close(af_engine* e);
+/* Close (if needed) and free the handle.  Safe on NULL. */
+void af_destroy(af_engine* e);
+
+/* Message of the engine's last failure ("" when none). */
+const char* af_last_error(const af_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AEROFLUX_CUDA_H */
