@@ -268,7 +268,7 @@ int reset_status(af_engine* e) {
 }
 
 void rec(af_engine* e, int idx) {
-    if (e->profiling) cudaEventRecord(e->ev[idx], e->stream);
+    if (e->profiling) cudaEventRecordWithFlags(e->ev[idx], e->stream, cudaEventRecordExternal);
 }
 
 void swap_fields(Fields& f) {
