@@ -81,6 +81,8 @@ SIGNATURES = {
     "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "af_seed_taylor_green": (C.c_int, [C.POINTER(AfConfig), C.c_double, C.c_double, C.c_uint64, C.c_uint64,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
+    "af_kinetic_energy_noalloc": (C.c_int, [C.POINTER(AfConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.POINTER(C.c_double), *_ERR]),
     "af_close": (C.c_int, [_E]),
     "af_destroy": (None, [_E]),
     "af_last_error": (C.c_char_p, [_E]),

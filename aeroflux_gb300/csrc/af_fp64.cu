@@ -8,11 +8,15 @@
 // between phases; here each stage is one grid-wide kernel and the join is the
 // kernel boundary.  Every stage is per-cell independent, so results do not
 // depend on the launch shape.
+#include "../../include/aeroflux_cuda.h"
 #include "af_internal.h"
 
 #include <math.h>
+#include <stdio.h>
 
 #include <algorithm>
+#include <cmath>
+#include <mutex>
 
 namespace af {
 namespace {
@@ -630,3 +634,108 @@ void launch_kinetic_energy(const Geom& g, const double* u, const double* v, cons
 }
 
 }  // namespace af
+
+// ---------------------------------------------------------------------------
+// Kinetic energy without any allocation.
+//
+// Some callers cannot allocate device memory while they run: hosts that hand
+// all device memory to their own pool up front and forbid cudaMalloc
+// afterwards, and latency-bound loops that cannot afford the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree.  This entry point runs
+// the same fixed-order reduction as af_kinetic_energy over caller-owned
+// device fields, with its scratch (one partial per z-plane plus the final
+// sum) in the file-scope array below.  Every GPU that loads the library holds
+// the array until the process exits.
+// ---------------------------------------------------------------------------
+namespace af {
+namespace {
+
+constexpr int kNoAllocMaxPlanes = 16384;  // 128 KiB of partials
+static __device__ __align__(256) double g_ke_scratch[kNoAllocMaxPlanes + 1];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_ke_scratch on the current device, resolved once per
+// device (host code only sees a host-side stand-in for the symbol).
+cudaError_t scratch_address(int dev, double** out) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t rc = cudaGetSymbolAddress(&p, g_ke_scratch);
+        if (rc != cudaSuccess) return rc;
+        g_scratch_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+void put(char* err, size_t errlen, const char* msg) {
+    if (err && errlen) snprintf(err, errlen, "%s", msg);
+}
+
+}  // namespace
+}  // namespace af
+
+extern "C" int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, const double* v, const double* w,
+                                         void* stream, double* out, char* err, size_t errlen) {
+    using namespace af;
+    if (!cfg || !u || !v || !w || !out) {
+        put(err, errlen, "aeroflux: kinetic energy without allocation: NULL argument");
+        return AF_ERR_ARG;
+    }
+    if (cfg->nx < 1 || cfg->ny < 1 || cfg->nz < 1 || cfg->ghost < 1 || !(cfg->h > 0) || std::isinf(cfg->h)) {
+        put(err, errlen, "aeroflux: kinetic energy without allocation: extents, ghost and h must be positive");
+        return AF_ERR_ARG;
+    }
+    if (cfg->nz > kNoAllocMaxPlanes || cfg->nx >= (1 << 20) || cfg->ny >= (1 << 20)) {
+        char m[160];
+        snprintf(m, sizeof m,
+                 "aeroflux: kinetic energy without allocation supports at most %d z-planes (and nx, ny < 2^20), "
+                 "got %lldx%lldx%lld",
+                 kNoAllocMaxPlanes, (long long)cfg->nx, (long long)cfg->ny, (long long)cfg->nz);
+        put(err, errlen, m);
+        return AF_ERR_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        put(err, errlen, "aeroflux: kinetic energy without allocation: no usable current device");
+        return AF_ERR_CUDA;
+    }
+    double* scratch = nullptr;
+    cudaError_t rc = scratch_address(dev, &scratch);
+    if (rc != cudaSuccess) {
+        put(err, errlen, cudaGetErrorString(rc));
+        return AF_ERR_CUDA;
+    }
+    Geom g{};
+    g.NX = (int)cfg->nx;
+    g.NY = (int)cfg->ny;
+    g.NZ = (int)cfg->nz;
+    g.G = (int)cfg->ghost;
+    const long long cx = cfg->nx + 2 * cfg->ghost, cy = cfg->ny + 2 * cfg->ghost;
+    g.u.sy = cx + 1;
+    g.u.sz = (cx + 1) * cy;
+    g.v.sy = cx;
+    g.v.sz = cx * (cy + 1);
+    g.w.sy = cx;
+    g.w.sz = cx * cy;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Every partial the final pass reads is rewritten by this call, so the
+    // array needs no clearing; concurrent calls on the GPU share it and race.
+    k_ke_planes<<<g.NZ, kKeThreads, 0, s>>>(g, u, v, w, scratch);
+    k_ke_final<<<1, kKeThreads, 0, s>>>(scratch, g.NZ, scratch + kNoAllocMaxPlanes);
+    double sum = 0;
+    if ((rc = cudaGetLastError()) != cudaSuccess ||
+        (rc = cudaMemcpyAsync(&sum, scratch + kNoAllocMaxPlanes, sizeof sum, cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (rc = cudaStreamSynchronize(s)) != cudaSuccess) {
+        put(err, errlen, cudaGetErrorString(rc));
+        return AF_ERR_CUDA;
+    }
+    const double h = cfg->h;
+    const double vol = h * h * h;
+    *out = 0.5 * sum * vol;
+    return AF_OK;
+}

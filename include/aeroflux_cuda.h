@@ -199,6 +199,24 @@ int af_device_fp64_rate(int device, double* fma_per_s);
 int af_seed_taylor_green(const af_config* cfg, double amp, double noise, uint64_t seed, uint64_t stream,
                          double* u, double* v, double* w);
 
+/* KineticEnergy of caller-owned device fields, allocating nothing.  No
+ * counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (hosts that hand all device memory to their own pool
+ * up front, loops that cannot afford cudaMalloc/cudaFree's implicit device
+ * synchronisation).  u, v, w are device pointers to the padded U, V, W fields
+ * of the MAC layout described by cfg (nx, ny, nz, ghost, h; other fields
+ * unused) on the current device; the sum is the fixed-order tree of
+ * af_kinetic_energy.  Its scratch is a static 128 KiB device array held by
+ * every GPU that loads the library until exit, so nz is limited to 16384
+ * z-planes (larger grids are rejected with AF_ERR_ARG and a message in err).
+ * The first call on a device resolves the array's address there; make that
+ * first call before any stream capture.  Enqueues on `stream` (a
+ * cudaStream_t, NULL for the default stream) and blocks until *out (host)
+ * holds the result.  All calls share the one array: calls that overlap on
+ * the GPU race. */
+int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, const double* v, const double* w,
+                              void* stream, double* out, char* err, size_t errlen);
+
 /* Close, aeroflux.go:419-439: release device memory.  Idempotent. */
 int af_close(af_engine* e);
 /* Close (if needed) and free the handle.  Safe on NULL. */
