@@ -332,17 +332,28 @@ void enqueue_step(af_engine* e) {
     rec(e, kEvEnd);
 }
 
-int build_graph(af_engine* e) {
+// Captures `body` on the engine stream and instantiates it.
+template <class F>
+int capture(af_engine* e, F body, cudaGraphExec_t* out) {
     cudaGraph_t graph = nullptr;
     AF_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(e);
+    body();
     cudaError_t rc = cudaStreamEndCapture(e->stream, &graph);
     if (rc != cudaSuccess) return cuda_fail(e, rc, "cudaStreamEndCapture");
-    rc = cudaGraphInstantiate(&e->graph[e->parity], graph, 0);
+    if (e->mixed) {
+        cudaError_t mrc = af::mixed_capture_error(e->mixed);
+        if (mrc != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return cuda_fail(e, mrc, "capturing the refinement loop");
+        }
+    }
+    rc = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (rc != cudaSuccess) return cuda_fail(e, rc, "cudaGraphInstantiate");
     return AF_OK;
 }
+
+int build_graph(af_engine* e) { return capture(e, [&] { enqueue_step(e); }, &e->graph[e->parity]); }
 
 // Rebuilds the reference's contained-fault text from a fault key: the fault
 // only fires on a NaN backtrace coordinate, so the tap indices follow from
@@ -586,7 +597,17 @@ int af_step(af_engine* e, int64_t nsteps) {
 int af_project(af_engine* e) {
     if (int rc = check_open(e)) return rc;
     if (int rc = reset_status(e)) return rc;
-    enqueue_project(e, e->fields(), 0);
+    if (e->mixed) {
+        // The refinement loop is a graph node: run the projection as a graph.
+        cudaGraphExec_t g = nullptr;
+        if (int rc = capture(e, [&] { enqueue_project(e, e->fields(), 0); }, &g)) return rc;
+        cudaError_t lrc = cudaGraphLaunch(g, e->stream);
+        cudaStreamSynchronize(e->stream);
+        cudaGraphExecDestroy(g);
+        if (lrc != cudaSuccess) return cuda_fail(e, lrc, "cudaGraphLaunch");
+    } else {
+        enqueue_project(e, e->fields(), 0);
+    }
     AF_CUDA(e, cudaGetLastError());
     return sync_and_check(e);
 }

@@ -18,5 +18,7 @@ void launch_sweep_mixed(MixedState* m, const Geom& g, int axis, const Fields& f,
 void enqueue_project_mixed(MixedState* m, const Geom& g, const af_config& c, const Fields& f, Status* st, int gate,
                            cudaStream_t s);
 void mixed_stats(MixedState* m, int64_t* passes, double* max_div);
+// First CUDA error met while capturing the refinement loop (then cleared).
+cudaError_t mixed_capture_error(MixedState* m);
 
 }  // namespace af

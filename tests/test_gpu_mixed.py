@@ -1,0 +1,114 @@
+"""Mixed-precision form: binary32 sweeps and inner multigrid solves inside
+binary64 iterative refinement.
+
+Its error is stated against the FP64 oracle with the red-black projection
+driven to convergence (max|div| ~1e-13): one projection must agree with it to
+~1e-11 relative in every velocity field (both are converged solutions of the
+same discrete problem), and whole Steps to ~1e-5 relative (binary32
+advection).  Every projection must reach the requested max|div|.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from aeroflux_gb300 import AF_PRECISION_MIXED, Config, New
+from aeroflux_gb300.workloads import taylor_green
+from tests.helpers import bits, make_pair, max_rel_diff, oracle_kwargs
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_cfg(n=(16, 16, 16), **kw):
+    nx, ny, nz = n
+    base = dict(NX=nx, NY=ny, NZ=nz, H=1.0 / max(n), DT=0.004, Viscosity=1e-5, Density=1.0,
+                Precision=AF_PRECISION_MIXED, DivTol=1e-10)
+    base.update(kw)
+    return Config(**base)
+
+
+def seeded(cfg, noise=0.01):
+    e = New(cfg)
+    u, v, w = taylor_green(e.Cfg, 1.0, noise)
+    for n, a in (("U", u), ("V", v), ("W", w)):
+        e.upload(n, a)
+    e.applyVelocityBC()
+    return e
+
+
+@pytest.mark.parametrize("n", [(16, 16, 16), (32, 32, 32), (24, 20, 18), (33, 17, 20), (48, 32, 96)])
+def test_projection_reaches_tolerance(n):
+    e = seeded(mixed_cfg(n))
+    before = e.MaxDivergence()
+    e.project()
+    passes, est = e.LastProjectionStats()
+    md = e.MaxDivergence()
+    print(f"{n}: max|div| {before:.3e} -> {md:.3e} in {passes} passes (estimate {est:.3e})")
+    assert md <= 1e-10
+    assert 1 <= passes <= e.Cfg.MaxRefine
+    e.Close()
+
+
+def test_projection_matches_converged_fp64_oracle():
+    # The same discrete projection, solved by the oracle's binary64 red-black
+    # sweeps run to convergence.
+    n = 16
+    cfg64 = Config(NX=n, NY=n, NZ=n, H=1 / n, DT=0.004, Viscosity=1e-5, Density=1.0, GaussSeidelIters=4000)
+    gpu64, orc = make_pair(cfg64, "tg", 1.0, 0.01)
+    orc.project()
+    assert orc.max_divergence() < 1e-12
+    e = seeded(mixed_cfg((n, n, n)))
+    e.project()
+    for i, name in ((1, "U"), (2, "V"), (3, "W")):
+        rel = max_rel_diff(e.download(name), orc.data(i))
+        print(f"projection {name}: max|diff|/max|ref| = {rel:.2e}")
+        assert rel < 1e-11
+    gpu64.Close()
+
+
+def test_steps_match_converged_fp64_oracle_within_binary32_error():
+    n, steps = 16, 5
+    cfg64 = Config(NX=n, NY=n, NZ=n, H=1 / n, DT=0.004, Viscosity=1e-5, Density=1.0, GaussSeidelIters=4000)
+    _, orc = make_pair(cfg64, "tg", 1.0, 0.01)
+    orc.step(steps)
+    e = seeded(mixed_cfg((n, n, n)))
+    e.Step(steps)
+    assert e.MaxDivergence() <= 1e-10
+    for i, name in ((1, "U"), (2, "V"), (3, "W")):
+        rel = max_rel_diff(e.download(name), orc.data(i))
+        print(f"{steps} steps {name}: max|diff|/max|ref| = {rel:.2e}")
+        assert rel < 1e-5
+
+
+def test_mixed_is_bit_identical_run_to_run():
+    outs = []
+    for _ in range(2):
+        e = seeded(mixed_cfg((24, 20, 18)))
+        e.Step(3)
+        outs.append(np.concatenate([bits(e.download(n)) for n in ("U", "V", "W", "P")]))
+        e.Close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_mixed_nan_is_a_contained_fault():
+    e = seeded(mixed_cfg((16, 16, 16)))
+    u = e.download("U")
+    u[5 + 6 * 19 + 7 * 19 * 18] = math.nan
+    e.upload("U", u)
+    with pytest.raises(Exception) as ex:
+        e.Step(2)
+    assert str(ex.value).startswith("aeroflux: guard-page fault contained")
+
+
+@pytest.mark.slow
+def test_mixed_256_cube_reaches_1e10_every_step():
+    e = seeded(mixed_cfg((256, 256, 256), DT=0.001))
+    for _ in range(3):
+        e.Step(1)
+        passes, _ = e.LastProjectionStats()
+        md = e.MaxDivergence()
+        print(f"256^3 mixed step: max|div| {md:.3e}, {passes} passes")
+        assert md <= 1e-10
+    for name in ("U", "V", "W", "P"):
+        assert np.all(np.isfinite(e.download(name)))
+    e.Close()
