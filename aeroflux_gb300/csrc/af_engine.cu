@@ -300,8 +300,14 @@ void enqueue_project_fp64(af_engine* e, const Fields& f, int gate) {
 }
 
 void enqueue_project(af_engine* e, const Fields& f, int gate) {
-    if (e->mixed) af::enqueue_project_mixed(e->mixed, e->geom, e->cfg, f, e->st, gate, e->stream);
-    else enqueue_project_fp64(e, f, gate);
+    if (e->mixed) {
+        // The profile's solve window spans the whole mixed projection.
+        rec(e, kEvRb + (gate == 3 ? 0 : 2));
+        af::enqueue_project_mixed(e->mixed, e->geom, e->cfg, f, e->st, gate, e->stream);
+        rec(e, kEvRb + (gate == 3 ? 1 : 3));
+    } else {
+        enqueue_project_fp64(e, f, gate);
+    }
 }
 
 void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {

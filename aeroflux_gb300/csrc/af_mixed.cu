@@ -31,6 +31,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -243,8 +244,8 @@ __global__ void k_mx_correct(Geom g, double* __restrict__ p, const float* __rest
 
 // One thread: decide whether another refinement pass runs.  Bounded by
 // max_refine, so the WHILE node always terminates.
-__global__ void k_mx_check(Ctl* ctl, cudaGraphConditionalHandle h, double scale, double thresh, unsigned max_refine,
-                           unsigned count_pass, Status* st, int gate) {
+__global__ void k_mx_check(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond, double scale, double thresh,
+                           unsigned max_refine, unsigned count_pass, Status* st, int gate) {
     const double r = __longlong_as_double((long long)ctl->maxr_bits);
     const double div = scale * r;
     ctl->last_div = div;
@@ -252,7 +253,7 @@ __global__ void k_mx_check(Ctl* ctl, cudaGraphConditionalHandle h, double scale,
     if (count_pass) ctl->passes += 1;
     const bool more = !gated(st, gate) && div > thresh && !isinf(div) && ctl->passes < max_refine;
     if (!more) ctl->stopped = 1;
-    cudaGraphSetConditional(h, more ? 1u : 0u);
+    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -403,6 +404,7 @@ struct MixedState {
     int coarse_sweeps = 64;
     unsigned max_refine = 30;
     double div_tol = 1e-10;
+    int fixed_passes = 0;   // > 0: unrolled loop of exactly this many passes
     cudaError_t capture_err = cudaSuccess;
 };
 
@@ -411,6 +413,9 @@ MixedState* mixed_create(const Geom& g, const af_config& c, cudaStream_t s, std:
     m->nu = (int)c.inner_sweeps;
     m->max_refine = (unsigned)c.max_refine;
     m->div_tol = c.div_tol;
+    // AEROFLUX_FIXED_REFINEMENT_PASSES=n replaces the WHILE node with n
+    // unrolled passes (for profilers and drivers without conditional nodes).
+    if (const char* fp = getenv("AEROFLUX_FIXED_REFINEMENT_PASSES")) m->fixed_passes = std::max(0, atoi(fp));
     // Levels: coarsen every axis that is even and >= 4 until none is or the
     // grid fits the one-block coarse solver.
     int nx = g.NX, ny = g.NY, nz = g.NZ;
@@ -425,7 +430,7 @@ MixedState* mixed_create(const Geom& g, const af_config& c, cudaStream_t s, std:
         L.cx = (nx % 2 == 0 && nx >= 4);
         L.cy = (ny % 2 == 0 && ny >= 4);
         L.cz = (nz % 2 == 0 && nz >= 4);
-        if (cells <= kCoarseMax && (cells <= 512 || !(L.cx || L.cy || L.cz))) { L.cx = L.cy = L.cz = 0; break; }
+        if (cells <= kCoarseMax && (cells <= 64 || !(L.cx || L.cy || L.cz))) { L.cx = L.cy = L.cz = 0; break; }
         if (!(L.cx || L.cy || L.cz) || m->nlev == 32) { L.cx = L.cy = L.cz = 0; break; }
         if (L.cx) { nx /= 2; wx *= 0.25f; }
         if (L.cy) { ny /= 2; wy *= 0.25f; }
@@ -439,7 +444,7 @@ MixedState* mixed_create(const Geom& g, const af_config& c, cudaStream_t s, std:
         m->coarse_sweeps = 0;
     } else {
         const int nmax = std::max(last.nx, std::max(last.ny, last.nz));
-        m->coarse_sweeps = std::min(1000, std::max(16, 2 * nmax * nmax));
+        m->coarse_sweeps = std::min(1000, std::max(8, 2 * nmax * nmax));
     }
     cudaError_t rc;
     if ((rc = cudaMalloc(&m->pool, total * sizeof(float))) != cudaSuccess ||
@@ -531,6 +536,27 @@ void enqueue_project_mixed(MixedState* m, const Geom& g, const af_config& c, con
     k_mx_init<<<1, 1, 0, s>>>(m->ctl);
     k_mx_residual<<<rgrid, 128, 0, s>>>(g, f.p, m->b, L0.r, L0.e, m->ctl, st, gate);
 
+    auto pass_body = [&](cudaStream_t bs, cudaGraphConditionalHandle h, int use_cond) {
+        // Later cycles continue from the current e0: their restriction takes
+        // the residual r0 - L(e0).
+        for (int k = 0; k < m->vcycles; ++k) vcycle(m, bs);
+        k_mx_correct<<<rgrid, 128, 0, bs>>>(g, f.p, L0.e, st, gate);
+        k_mx_residual<<<rgrid, 128, 0, bs>>>(g, f.p, m->b, L0.r, L0.e, m->ctl, st, gate);
+        k_mx_check<<<1, 1, 0, bs>>>(m->ctl, h, use_cond, scale, thresh, m->max_refine, 1u, st, gate);
+    };
+    auto finish = [&]() {
+        launch_pressure_bc_fp64(g, f.p, st, gate, s);
+        launch_gradient_fp64(g, f, c.dt / (c.density * c.h), st, gate, s);
+        launch_velocity_bc(g, f.u, f.v, f.w, st, gate, s);
+    };
+    if (m->fixed_passes > 0) {
+        cudaGraphConditionalHandle none = 0;
+        k_mx_check<<<1, 1, 0, s>>>(m->ctl, none, 0, scale, thresh, m->max_refine, 0u, st, gate);
+        for (int k = 0; k < m->fixed_passes; ++k) pass_body(s, none, 0);
+        finish();
+        return;
+    }
+
     // The WHILE node: add it to the capturing graph after the nodes so far.
     cudaStreamCaptureStatus cs;
     cudaGraph_t graph = nullptr;
@@ -546,7 +572,7 @@ void enqueue_project_mixed(MixedState* m, const Geom& g, const af_config& c, con
         m->capture_err = rc;
         return;
     }
-    k_mx_check<<<1, 1, 0, s>>>(m->ctl, h, scale, thresh, m->max_refine, 0u, st, gate);
+    k_mx_check<<<1, 1, 0, s>>>(m->ctl, h, 1, scale, thresh, m->max_refine, 0u, st, gate);
     rc = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
     if (rc != cudaSuccess) {
         m->capture_err = rc;
@@ -568,12 +594,7 @@ void enqueue_project_mixed(MixedState* m, const Geom& g, const af_config& c, con
         m->capture_err = rc;
         return;
     }
-    // Later cycles continue from the current e0: their restriction takes the
-    // residual r0 - L(e0).
-    for (int k = 0; k < m->vcycles; ++k) vcycle(m, m->body);
-    k_mx_correct<<<rgrid, 128, 0, m->body>>>(g, f.p, L0.e, st, gate);
-    k_mx_residual<<<rgrid, 128, 0, m->body>>>(g, f.p, m->b, L0.r, L0.e, m->ctl, st, gate);
-    k_mx_check<<<1, 1, 0, m->body>>>(m->ctl, h, scale, thresh, m->max_refine, 1u, st, gate);
+    pass_body(m->body, h, 1);
     cudaGraph_t body_out = nullptr;
     if ((rc = cudaStreamEndCapture(m->body, &body_out)) != cudaSuccess) {
         m->capture_err = rc;
@@ -584,9 +605,7 @@ void enqueue_project_mixed(MixedState* m, const Geom& g, const af_config& c, con
         m->capture_err = rc;
         return;
     }
-    launch_pressure_bc_fp64(g, f.p, st, gate, s);
-    launch_gradient_fp64(g, f, c.dt / (c.density * c.h), st, gate, s);
-    launch_velocity_bc(g, f.u, f.v, f.w, st, gate, s);
+    finish();
 }
 
 void mixed_stats(MixedState* m, int64_t* passes, double* max_div) {

@@ -213,53 +213,62 @@ def bench_reference(args):
     return 0
 
 
-def bench_ours(args):
-    import numpy as np
-
-    from aeroflux_gb300 import _lib as L
+def new_engine(precision: int, local: int, rank: int, div_tol: float = 0.0):
     from aeroflux_gb300 import New
     from aeroflux_gb300.workloads import taylor_green
-
-    rank, local, world = rank_info()
-    dist = Dist(world)
-    wl = base_config()
-    cfg = wl.config(Device=local)
+    cfg = base_config().config(Device=local, Precision=precision, DivTol=div_tol)
     e = New(cfg)
     u, v, w = taylor_green(e.Cfg, 1.0, NOISE, 42, rank)
     for name, a in (("U", u), ("V", v), ("W", w)):
         e.upload(name, a)
     e.applyVelocityBC()
-    e.Profile(True)
-    for _ in range(args.warmup):
-        e.Step(1)
+    return e, (u, v, w)
 
-    # --- device-timed region: exactly K steps --------------------------------
-    clocks = ClockSampler(local)
+
+def device_timed(e, steps: int, warmup: int, dist, clocks=None):
+    """Exactly `steps` Steps timed by the step graph's event nodes (device
+    time on the engine's stream), after `warmup` untimed Steps."""
+    e.Profile(True)
+    for _ in range(warmup):
+        e.Step(1)
     dist.barrier()
-    clocks.start()
-    time.sleep(0.3)
-    dev_ms = rb_ms = sw_ms = 0.0
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    dev_ms = solve_ms = sw_ms = 0.0
+    passes = []
     t0 = time.perf_counter()
     prof = None
-    for _ in range(args.steps):
+    for _ in range(steps):
         e.Step(1)  # synchronous: returns after the step graph completes
         prof = e.LastStepProfile()
         dev_ms += prof.step_ms
-        rb_ms += prof.rbgs_ms
+        solve_ms += prof.rbgs_ms
         sw_ms += prof.sweep_ms
+        passes.append(e.LastProjectionStats()[0])
     wall = time.perf_counter() - t0
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
     dist.barrier()
-    dev_s = dist.max(dev_ms / 1e3)
+    e.Profile(False)
+    return {"dev_s": dist.max(dev_ms / 1e3), "wall_s": wall, "solve_ms": solve_ms / steps, "sweep_ms": sw_ms / steps,
+            "launches": prof.kernel_launches, "rbgs_launches": prof.rbgs_launches, "passes": passes, "clocks": clk}
+
+
+def bench_ours(args):
+    from aeroflux_gb300 import _lib as L
+
+    rank, local, world = rank_info()
+    dist = Dist(world)
     cells = N ** 3
-    value = cells * args.steps * world / dev_s
-    launches = prof.kernel_launches * args.steps
-    rb_launch_s = rb_ms / 1e3 / (prof.rbgs_launches * args.steps)
-    sweep_ms_per = sw_ms / (6 * args.steps)
-    md = e.MaxDivergence()
+
+    # --- plain FP64 (the headline workload) ---------------------------------
+    e, (u, v, w) = new_engine(L.AF_PRECISION_FP64, local, rank)
+    t = device_timed(e, args.steps, args.warmup, dist, ClockSampler(local))
+    value = cells * args.steps * world / t["dev_s"]
+    md_plain = e.MaxDivergence()
+    rb_launch_s = t["solve_ms"] / 1e3 / t["rbgs_launches"]
 
     # --- end to end through the C ABI with host buffers ---------------------
-    e.Profile(False)
     try:
         import torch
         pin = torch.cuda.is_available()
@@ -268,8 +277,8 @@ def bench_ours(args):
     host = []
     for a in (u, v, w):
         if pin:
-            t = torch.from_numpy(a).pin_memory()
-            host.append((t, t.data_ptr(), a.size))
+            tt = torch.from_numpy(a).pin_memory()
+            host.append((tt, tt.data_ptr(), a.size))
         else:
             host.append((a, a.ctypes.data, a.size))
     lib = L.lib()
@@ -290,6 +299,7 @@ def bench_ours(args):
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_val = cells * e2e_steps * world / e2e_s
     h2d = 8 * (u.size + v.size + w.size)
+    e.Close()
 
     # --- roofline of the dominant kernel (one red-black colour sweep) --------
     peak, peak_kind = measured_peaks()
@@ -301,13 +311,27 @@ def bench_ours(args):
     fp64_inst = 9 * cells / 2  # per update: 5 adds, 1 sub, and mul+2 FMA for the exact /6
     fp64_ach = fp64_inst / rb_launch_s
 
+    # --- mixed precision, at 1e-10 and at the plain form's own max|div| ------
+    mixed = {}
+    for label, tol in (("mixed", 1e-10), ("mixed_same_div_tol", max(md_plain, 1e-10))):
+        em, _ = new_engine(L.AF_PRECISION_MIXED, local, rank, tol)
+        tm = device_timed(em, args.steps, args.warmup, dist)
+        mv = cells * args.steps * world / tm["dev_s"]
+        mixed[label] = {"value": mv, "unit": UNIT, "ms_per_step": tm["dev_s"] * 1e3 / args.steps,
+                        "div_tol": tol, "max_divergence_after": em.MaxDivergence(),
+                        "refinement_passes_last_projection": tm["passes"],
+                        "stages_ms_per_step": {"projections": tm["solve_ms"], "sweeps": tm["sweep_ms"]},
+                        "speedup_vs_plain": mv / value,
+                        "dtype": "f32 sweeps and inner multigrid, f64 state/residual/accumulator"}
+        em.Close()
+
     dist.close()
     if rank != 0:
         return 0
     line = common_fields(args, world)
     line.update({
-        "value": value, "ms_per_step": dev_s * 1e3 / args.steps, "wall_ms_per_step": wall * 1e3 / args.steps,
-        "gpu_launches": launches,
+        "value": value, "ms_per_step": t["dev_s"] * 1e3 / args.steps, "wall_ms_per_step": t["wall_s"] * 1e3 / args.steps,
+        "gpu_launches": t["launches"] * args.steps,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8,
                 "steps": e2e_steps, "host_memory": "pinned" if pin else "pageable"},
         "roofline": {"bound": "hbm", "kernel": "k_rbgs_fp64 (one colour sweep)", "achieved": achieved,
@@ -317,10 +341,10 @@ def bench_ours(args):
                      "fp64_pipe": {"achieved": fp64_ach, "peak": fma_rate.value, "unit": "FP64 inst/s",
                                    "frac": fp64_ach / fma_rate.value if fma_rate.value else None,
                                    "inst_per_update": 9}},
-        "stages_ms_per_step": {"rbgs": rb_ms / args.steps, "sweeps": sw_ms / args.steps,
-                               "sweep_each": sweep_ms_per, "step": dev_s * 1e3 / args.steps},
-        "max_divergence_after": md,
-        "clocks": clk,
+        "stages_ms_per_step": {"rbgs": t["solve_ms"], "sweeps": t["sweep_ms"], "step": t["dev_s"] * 1e3 / args.steps},
+        "max_divergence_after": md_plain,
+        "clocks": t["clocks"],
+        **mixed,
     })
     if world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads()
@@ -329,7 +353,6 @@ def bench_ours(args):
                                 "sample": f"1 Step of the {N}^3 workload on the CPU oracle (C restatement of "
                                           f"the Go path), {threads} worker threads, {sec:.1f} s"}
     print(json.dumps(line), flush=True)
-    e.Close()
     return 0
 
 

@@ -175,8 +175,9 @@ int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div);
 typedef struct af_step_profile {
     double step_ms;           /* whole step */
     double sweep_ms;          /* the six advection/diffusion sweeps (BC passes excluded) */
-    double rbgs_ms;           /* the red-black sweeps of both projections */
-    int64_t rbgs_launches;    /* red-black kernel launches per step */
+    double rbgs_ms;           /* FP64: the red-black sweeps of both projections;
+                                 MIXED: both projections (refinement included) */
+    int64_t rbgs_launches;    /* FP64: red-black kernel launches per step */
     int64_t kernel_launches;  /* kernel launches per step */
 } af_step_profile;
 

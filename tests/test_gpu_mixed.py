@@ -3,9 +3,10 @@ binary64 iterative refinement.
 
 Its error is stated against the FP64 oracle with the red-black projection
 driven to convergence (max|div| ~1e-13): one projection must agree with it to
-~1e-11 relative in every velocity field (both are converged solutions of the
-same discrete problem), and whole Steps to ~1e-5 relative (binary32
-advection).  Every projection must reach the requested max|div|.
+1e-9 relative in every velocity field (both are converged solutions of the
+same discrete problem, so they differ at the level of the 1e-10 divergence
+tolerance, orders below binary32 round-off), and whole Steps to ~1e-5
+relative (binary32 advection).  Every projection must reach the requested max|div|.
 """
 import math
 
@@ -62,7 +63,9 @@ def test_projection_matches_converged_fp64_oracle():
     for i, name in ((1, "U"), (2, "V"), (3, "W")):
         rel = max_rel_diff(e.download(name), orc.data(i))
         print(f"projection {name}: max|diff|/max|ref| = {rel:.2e}")
-        assert rel < 1e-11
+        # Both reach max|div| <= 1e-10; their fields then differ at the level
+        # of that tolerance, far below binary32 round-off (~1e-7).
+        assert rel < 1e-9
     gpu64.Close()
 
 
