@@ -79,6 +79,25 @@ SIGNATURES = {
     "af_profile": (C.c_int, [_E, C.c_int]),
     "af_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
     "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "af_batch_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.POINTER(_E), *_ERR]),
+    "af_batch_slot_bytes": (C.c_int, [C.POINTER(AfConfig), C.POINTER(C.c_int64)]),
+    "af_batch_assign": (C.c_int, [_E, C.POINTER(AfConfig), C.POINTER(C.c_int64)]),
+    "af_batch_release": (C.c_int, [_E, C.c_int64]),
+    "af_batch_set_active": (C.c_int, [_E, C.c_int64, C.c_int]),
+    "af_batch_get_config": (C.c_int, [_E, C.c_int64, C.POINTER(AfConfig)]),
+    "af_batch_field_info": (C.c_int, [_E, C.c_int64, C.c_int, C.POINTER(AfFieldDesc)]),
+    "af_batch_field_upload": (C.c_int, [_E, C.c_int64, C.c_int, C.c_void_p, C.c_size_t]),
+    "af_batch_field_download": (C.c_int, [_E, C.c_int64, C.c_int, C.c_void_p, C.c_size_t]),
+    "af_batch_apply_velocity_bc": (C.c_int, [_E]),
+    "af_batch_step": (C.c_int, [_E, C.c_int64]),
+    "af_batch_slot_status": (C.c_int, [_E, C.c_int64, C.POINTER(C.c_int32), *_ERR]),
+    "af_batch_max_divergence": (C.c_int, [_E, C.c_int64, C.POINTER(C.c_double)]),
+    "af_batch_projection_stats": (C.c_int, [_E, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "af_batch_tune": (C.c_int, [_E, C.c_int32, *_ERR]),
+    "af_batch_profile": (C.c_int, [_E, C.c_int]),
+    "af_batch_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
+    "af_batch_destroy": (None, [_E]),
+    "af_batch_last_error": (C.c_char_p, [_E]),
     "af_seed_taylor_green": (C.c_int, [C.POINTER(AfConfig), C.c_double, C.c_double, C.c_uint64, C.c_uint64,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "af_kinetic_energy_noalloc": (C.c_int, [C.POINTER(AfConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

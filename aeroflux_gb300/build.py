@@ -27,7 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "af_engine.cu": ["--fmad=false"],
     "af_fp64.cu": ["--fmad=false"],
-    "af_mixed.cu": [],
+    "af_batch.cu": [],
     "af_workload.cu": [],
 }
 

@@ -1,0 +1,1374 @@
+// af_batch.cu -- batched mixed-precision fractional step.
+//
+// Many independent grids (slots) of uneven sizes step together.  Every stage
+// is ONE persistent launch over a device-side work list: per stage, a prefix
+// array gives each slot's number of tiles, a block finds its slot by binary
+// search and processes one tile of that slot's iteration space, and the grid
+// (a fixed multiple of the SM count) strides over all tiles.  Because the
+// work lists live in device memory, slots can be assigned, released,
+// activated and deactivated between steps without recapturing the step
+// graph (continuous batching); the graph is recaptured only when the
+// deepest multigrid hierarchy grows or the launch shapes are retuned.
+//
+// Arithmetic (see af_mixed.h): binary32 advection/diffusion with integer-pipe
+// conversions; binary64 divergence, residual, pressure accumulator, gradient
+// and BCs (bit-identical to the FP64 form's cells); binary32 multigrid
+// V-cycles with red-black smoothing inside binary64 refinement.  The
+// refinement loop is one WHILE node for the whole batch: it runs while any
+// slot is unconverged, and a converged slot skips every later pass, so each
+// slot performs exactly the passes it performs alone.  Every cell's result is
+// independent of the tile that computes it, and reductions are exact maxima
+// or fixed trees over one slot, so a slot's bits do not depend on the other
+// slots or on the tuned launch shapes.
+#include "af_batch.h"
+#include "af_cells.cuh"
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+namespace af {
+namespace {
+
+using namespace cells;
+
+constexpr int kMaxLev = 16;
+constexpr int kCoarseThreads = 512;
+constexpr int kCoarseMax = 4096;
+
+struct Lvl {
+    int nx, ny, nz;
+    float wx, wy, wz;   // (h0 / h_axis)^2
+    int cx, cy, cz;     // 1 when the axis coarsens into the next level
+    float* e;
+    float* r;
+};
+
+struct Ctl {
+    unsigned long long maxr_bits;  // max |r| of the current pass (binary64 bits)
+    unsigned int passes;
+    unsigned int stopped;
+    double last_div;               // dt/(rho h^2) * max|r| at the last check
+};
+
+struct InstDev {
+    Geom g;
+    double* slot[8];   // arena field slots P, U, V, W, Div, Tmp0, Tmp1, Tmp2
+    double* b;         // h^2 * Div, P-shaped
+    float dt_invh;     // (DT/2)/H for the sweeps
+    float lam;         // nu*(DT/2)/H^2
+    double div_scale;  // rho/(DT*H)
+    double h2;
+    double grad_scale;  // DT/(rho*H)
+    double res_scale;   // DT/(rho*H^2): max|div| per unit residual
+    double thresh;      // 0.5 * div_tol
+    unsigned max_refine;
+    int nlev;
+    int coarse_sweeps;  // > 0: one-block coarse solve; 0: smoothing at the coarsest level
+    int parity;         // 1 when U/V/W live in the Tmp slots
+    int active;
+    Lvl lev[kMaxLev];
+};
+
+// Stage ids.  Level stages take kMaxLev consecutive ids.
+enum {
+    S_BC = 0, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD, S_COARSE,
+    S_SMOOTH = 7,
+    S_RESTRICT = S_SMOOTH + kMaxLev,
+    S_PROLONG = S_RESTRICT + kMaxLev,
+    S_BIGCOARSE = S_PROLONG + kMaxLev,
+    S_COUNT = S_BIGCOARSE + kMaxLev
+};
+
+struct Shape {
+    int tpb = 256;   // threads per block
+    int ept = 1;     // elements per thread
+    int bpsm = 8;    // persistent blocks per SM
+};
+
+// A stage's device work list: prefix[0..n] of tiles per slot.
+struct Tab {
+    const int* prefix;
+    int n;
+    int ept;
+};
+
+__device__ __forceinline__ int find_slot(const int* prefix, int n, int item) {
+    int lo = 0, hi = n;  // prefix[lo] <= item < prefix[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (prefix[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Loop over this block's tiles; `s` is the slot, `first` the first element
+// of the tile; body sees element index `el` (< the slot's count, checked by
+// the body).
+#define FOR_TILES(tab)                                                                   \
+    for (int item = blockIdx.x, total = (tab).prefix[(tab).n]; item < total; item += gridDim.x) { \
+        const int s = find_slot((tab).prefix, (tab).n, item);                            \
+        const long long first = (long long)(item - (tab).prefix[s]) * blockDim.x * (tab).ept;
+#define FOR_ELEMS(tab) \
+        for (int k_ = 0; k_ < (tab).ept; ++k_) {      \
+            const long long el = first + (long long)k_ * blockDim.x + threadIdx.x;
+#define END_ELEMS }
+#define END_TILES }
+
+__device__ __forceinline__ double* cur(const InstDev& I, int field, int parity) {
+    const int p = parity ^ I.parity;
+    if (!p || field == 0 || field == 4) return I.slot[field];
+    return I.slot[field <= 3 ? field + 4 : field - 4];
+}
+
+// --- counts of each stage's iteration space -------------------------------
+__host__ __device__ inline long long bc_count(const Geom& g) {
+    const long long N[3][3] = {{g.NX, g.NY, g.NZ}, {g.NY, g.NX, g.NZ}, {g.NZ, g.NX, g.NY}};
+    long long c = 0;
+    for (int k = 0; k < 3; ++k) c += 2 * N[k][1] * N[k][2] + 2 * (N[k][0] + 1) * N[k][2] + 2 * (N[k][0] + 1) * (N[k][1] + 2);
+    return c;
+}
+__host__ __device__ inline long long face_box(const Geom& g) {
+    return (long long)(g.NX + 1) * (g.NY + 1) * 3 * (g.NZ + 1);
+}
+__host__ __device__ inline long long pbc_count(const Geom& g) {
+    return 2ll * g.NY * g.NZ + 2ll * (g.NX + 2) * g.NZ + 2ll * (g.NX + 2) * (g.NY + 2);
+}
+__host__ __device__ inline long long half_box(const Lvl& L) { return (long long)((L.nx + 1) / 2) * L.ny * L.nz; }
+__host__ __device__ inline long long lvl_cells(const Lvl& L) { return (long long)L.nx * L.ny * L.nz; }
+
+// --- binary64 stages (bit-identical to the FP64 form's cells) -------------
+__global__ void kb_bc(const InstDev* inst, Status* st, Tab tab, int parity, int gate) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], gate)) continue;
+    double* u = cur(I, 1, parity);
+    double* v = cur(I, 2, parity);
+    double* w = cur(I, 3, parity);
+    const long long n = bc_count(I.g);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    long long i = el;
+    int comp = 0, set = 0;
+    for (;;) {
+        const BcComp c = bc_comp(I.g, comp, u, v, w);
+        const long long cnt = bc_set_count(c, set);
+        if (i < cnt) {
+            bc_cell(c, I.g.G, set, i);
+            break;
+        }
+        i -= cnt;
+        if (++set == 3) { set = 0; ++comp; }
+    }
+    END_ELEMS
+    END_TILES
+}
+
+__global__ void kb_div(const InstDev* inst, Status* st, Tab tab, int parity, int gate) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], gate)) continue;
+    const Geom& g = I.g;
+    const long long n = (long long)g.p.nx * g.p.ny * g.p.nz;
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    const int x = (int)(el % g.p.nx);
+    const long long r = el / g.p.nx;
+    div_cell(g, cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.slot[0], I.slot[4], I.b, I.div_scale,
+             I.h2, true, x, (int)(r % g.p.ny), (int)(r / g.p.ny));
+    END_ELEMS
+    END_TILES
+}
+
+__global__ void kb_pbc(const InstDev* inst, Status* st, Tab tab, int gate) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], gate)) continue;
+    const Geom& g = I.g;
+    const long long c0 = pbc_set_count(g, 0), c1 = pbc_set_count(g, 1), n = pbc_count(g);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    if (el < c0) pbc_cell(g, I.slot[0], 0, el);
+    else if (el < c0 + c1) pbc_cell(g, I.slot[0], 1, el - c0);
+    else pbc_cell(g, I.slot[0], 2, el - c0 - c1);
+    END_ELEMS
+    END_TILES
+}
+
+__device__ __forceinline__ bool face_of(const Geom& g, long long el, int* c, int* x, int* y, int* z) {
+    *x = g.G + (int)(el % (g.NX + 1));
+    long long r = el / (g.NX + 1);
+    *y = g.G + (int)(r % (g.NY + 1));
+    r /= (g.NY + 1);
+    *c = (int)(r / (g.NZ + 1));
+    *z = g.G + (int)(r % (g.NZ + 1));
+    return *x < g.G + g.NX + (*c == 0) && *y < g.G + g.NY + (*c == 1) && *z < g.G + g.NZ + (*c == 2);
+}
+
+__global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, int gate) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], gate)) continue;
+    const long long n = face_box(I.g);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    int c, x, y, z;
+    if (face_of(I.g, el, &c, &x, &y, &z))
+        grad_face(I.g, I.slot[0], cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.grad_scale, c, x, y, z);
+    END_ELEMS
+    END_TILES
+}
+
+template <int AX>
+__global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, int phase) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], phase)) continue;
+    const long long n = face_box(I.g);
+    const double* u = cur(I, 1, parity);
+    const double* v = cur(I, 2, parity);
+    const double* w = cur(I, 3, parity);
+    double* tu = cur(I, 5, parity);
+    double* tv = cur(I, 6, parity);
+    double* tw = cur(I, 7, parity);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    int c, x, y, z;
+    if (face_of(I.g, el, &c, &x, &y, &z) && !mx_sweep_face<AX>(I.g, u, v, w, tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
+        atomicMin(&st[s].fault_gate, st[s].step * 8u + (unsigned)phase);
+        atomicMin(&st[s].fault_key, fault_key(c, x, y, z));
+    }
+    END_ELEMS
+    END_TILES
+}
+
+__global__ void kb_tick(const InstDev* inst, Status* st, int n) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        if (inst[s].active) st[s].step += 1;
+}
+
+// --- refinement control ---------------------------------------------------
+__global__ void kb_init(const InstDev* inst, Ctl* ctl, int n) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        ctl[s].maxr_bits = 0;
+        ctl[s].passes = 0;
+        ctl[s].stopped = inst[s].active ? 0u : 1u;
+        ctl[s].last_div = 0;
+    }
+}
+
+// r = b - L(p) in binary64 over the interior, r (binary32) for the inner
+// solve, inner solution zeroed, max|r| reduced per slot.  In the loop a
+// converged slot is skipped.
+__global__ void kb_residual(const InstDev* inst, Status* st, Ctl* ctl, Tab tab, int gate, int in_loop) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (gated(&st[s], gate) || (in_loop && ctl[s].stopped)) continue;
+    const Geom& g = I.g;
+    const double* p = I.slot[0];
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    unsigned long long m = 0;
+    FOR_ELEMS(tab)
+    if (el < n) {
+        const int xi = (int)(el % g.NX);
+        const long long r2 = el / g.NX;
+        const int yi = (int)(r2 % g.NY), zi = (int)(r2 / g.NY);
+        const long long sy = g.p.sy, sz = g.p.sz;
+        const long long i = (g.G + xi) + (g.G + yi) * sy + (g.G + zi) * sz;
+        const double pc = p[i];
+        const double xm = xi > 0 ? p[i - 1] : pc;
+        const double xp = xi < g.NX - 1 ? p[i + 1] : pc;
+        const double ym = yi > 0 ? p[i - sy] : pc;
+        const double yp = yi < g.NY - 1 ? p[i + sy] : pc;
+        const double zm = zi > 0 ? p[i - sz] : pc;
+        const double zp = zi < g.NZ - 1 ? p[i + sz] : pc;
+        const double res = I.b[i] - fma(-6.0, pc, ((xm + xp) + (ym + yp)) + (zm + zp));
+        I.lev[0].r[el] = f64_to_f32(res);
+        I.lev[0].e[el] = 0.0f;
+        // |res| and NaN tested on the bit pattern (integer pipe); NaN reads as
+        // +Inf so the loop stops.
+        const unsigned long long a = (unsigned long long)__double_as_longlong(res) & ~kSign;
+        const unsigned long long v = a > 0x7FF0000000000000ull ? 0x7FF0000000000000ull : a;
+        m = v > m ? v : m;
+    }
+    END_ELEMS
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctl[s].maxr_bits, m);
+    END_TILES
+}
+
+__global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    if (ctl[s].stopped) continue;
+    const Geom& g = I.g;
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    const int xi = (int)(el % g.NX);
+    const long long r2 = el / g.NX;
+    const long long i = (g.G + xi) + (g.G + (int)(r2 % g.NY)) * g.p.sy + (g.G + (int)(r2 / g.NY)) * g.p.sz;
+    I.slot[0][i] += f32_to_f64(I.lev[0].e[el]);
+    END_ELEMS
+    END_TILES
+}
+
+// One block: per slot, whether another refinement pass runs; the WHILE
+// condition is "any slot continues".  Bounded by each slot's max_refine.
+__global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaGraphConditionalHandle h, int use_cond,
+                         int count_pass, int gate) {
+    int any = 0;
+    for (int s = threadIdx.x; s < n; s += blockDim.x) {
+        const InstDev& I = inst[s];
+        if (!I.active) continue;
+        Ctl& c = ctl[s];
+        const double r = __longlong_as_double((long long)c.maxr_bits);
+        c.maxr_bits = 0;
+        if (c.stopped) continue;
+        const double div = I.res_scale * r;
+        c.last_div = div;
+        if (count_pass) c.passes += 1;
+        const bool more = !gated(&st[s], gate) && div > I.thresh && !isinf(div) && c.passes < I.max_refine;
+        if (!more) c.stopped = 1;
+        any |= more ? 1 : 0;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+// --- binary32 multigrid ---------------------------------------------------
+__device__ __forceinline__ long long lidx(int x, int y, int z, int nx, int ny) {
+    return x + (long long)nx * (y + (long long)ny * z);
+}
+
+__global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color) {
+    FOR_TILES(tab)
+    if (ctl[s].stopped) continue;
+    const Lvl L = inst[s].lev[l];
+    const int hx = (L.nx + 1) / 2;
+    const long long n = (long long)hx * L.ny * L.nz;
+    const long long nxy = (long long)L.nx * L.ny;
+    const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    const int k = (int)(el % hx);
+    const long long r = el / hx;
+    const int y = (int)(r % L.ny), z = (int)(r / L.ny);
+    const int x = (((y + z) & 1) != color ? 1 : 0) + 2 * k;
+    if (x < L.nx) {
+        const long long i = lidx(x, y, z, L.nx, L.ny);
+        const float c = L.e[i];
+        const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c);
+        const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c);
+        const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c);
+        L.e[i] = (L.wx * sx + L.wy * sy + L.wz * sz - L.r[i]) * inv;
+    }
+    END_ELEMS
+    END_TILES
+}
+
+__device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) {
+    const long long nxy = (long long)L.nx * L.ny;
+    const long long i = lidx(x, y, z, L.nx, L.ny);
+    const float c = L.e[i];
+    const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c) - 2.0f * c;
+    const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c) - 2.0f * c;
+    const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c) - 2.0f * c;
+    return L.r[i] - (L.wx * sx + L.wy * sy + L.wz * sz);
+}
+
+// Coarse rhs = mean of the children's residuals; coarse solution = 0.
+__global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
+    FOR_TILES(tab)
+    if (ctl[s].stopped) continue;
+    const Lvl F = inst[s].lev[l];
+    const Lvl C = inst[s].lev[l + 1];
+    const long long n = lvl_cells(C);
+    const int ex = F.cx ? 2 : 1, ey = F.cy ? 2 : 1, ez = F.cz ? 2 : 1;
+    const float inv = 1.0f / (float)(ex * ey * ez);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    const int X = (int)(el % C.nx);
+    const long long r = el / C.nx;
+    const int Y = (int)(r % C.ny), Z = (int)(r / C.ny);
+    float sum = 0.0f;
+    for (int dz = 0; dz < ez; ++dz)
+        for (int dy = 0; dy < ey; ++dy)
+            for (int dx = 0; dx < ex; ++dx) sum += mg_residual(F, X * ex + dx, Y * ey + dy, Z * ez + dz);
+    C.r[el] = sum * inv;
+    C.e[el] = 0.0f;
+    END_ELEMS
+    END_TILES
+}
+
+// e_fine += cell-centred trilinear interpolation of e_coarse: per coarsened
+// axis the parent weighs 3/4 and the next coarse cell toward the fine cell
+// 1/4 (clamped at the walls, the Neumann reflection).
+__global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
+    FOR_TILES(tab)
+    if (ctl[s].stopped) continue;
+    const Lvl F = inst[s].lev[l];
+    const Lvl C = inst[s].lev[l + 1];
+    const long long n = lvl_cells(F);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    const int x = (int)(el % F.nx);
+    const long long r = el / F.nx;
+    const int y = (int)(r % F.ny), z = (int)(r / F.ny);
+    int X0 = x, X1 = x, Y0 = y, Y1 = y, Z0 = z, Z1 = z;
+    float ax = 1.0f, ay = 1.0f, az = 1.0f;
+    if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
+    if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
+    if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
+    auto E = [&](int i, int j, int k) { return C.e[lidx(i, j, k, C.nx, C.ny)]; };
+    const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
+    const float v = az * (ay * (ax * E(X0, Y0, Z0) + bx * E(X1, Y0, Z0)) + by * (ax * E(X0, Y1, Z0) + bx * E(X1, Y1, Z0))) +
+                    bz * (ay * (ax * E(X0, Y0, Z1) + bx * E(X1, Y0, Z1)) + by * (ax * E(X0, Y1, Z1) + bx * E(X1, Y1, Z1)));
+    F.e[el] += v;
+    END_ELEMS
+    END_TILES
+}
+
+__device__ float block_sum(float v, float* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float s = threadIdx.x < kCoarseThreads / 32 ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) red[0] = s;
+    }
+    __syncthreads();
+    const float s = red[0];
+    __syncthreads();
+    return s;
+}
+
+// Coarsest level of one slot per block: remove the mean of r (a Neumann
+// problem is solvable only for zero-mean data), red-black sweeps from zero
+// in shared memory, remove the mean of e.  Sums use a fixed tree.
+__global__ void __launch_bounds__(kCoarseThreads) kb_coarse(const InstDev* inst, const Ctl* ctl, Tab tab) {
+    __shared__ float se[kCoarseMax];
+    __shared__ float sr[kCoarseMax];
+    __shared__ float red[32];
+    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
+        const int s = find_slot(tab.prefix, tab.n, item);
+        if (ctl[s].stopped) continue;
+        const InstDev& I = inst[s];
+        const Lvl L = I.lev[I.nlev - 1];
+        const int n = L.nx * L.ny * L.nz;
+        float part = 0.0f;
+        for (int i = threadIdx.x; i < n; i += kCoarseThreads) {
+            sr[i] = L.r[i];
+            se[i] = 0.0f;
+            part += sr[i];
+        }
+        const float mean_r = block_sum(part, red) / (float)n;
+        for (int i = threadIdx.x; i < n; i += kCoarseThreads) sr[i] -= mean_r;
+        __syncthreads();
+        const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
+        const int nxy = L.nx * L.ny;
+        for (int it = 0; it < 2 * I.coarse_sweeps; ++it) {
+            const int color = it & 1;
+            for (int i = threadIdx.x; i < n; i += kCoarseThreads) {
+                const int x = i % L.nx, y = (i / L.nx) % L.ny, z = i / nxy;
+                if (((x + y + z) & 1) != color) continue;
+                const float c = se[i];
+                const float sx = (x > 0 ? se[i - 1] : c) + (x < L.nx - 1 ? se[i + 1] : c);
+                const float sy = (y > 0 ? se[i - L.nx] : c) + (y < L.ny - 1 ? se[i + L.nx] : c);
+                const float sz = (z > 0 ? se[i - nxy] : c) + (z < L.nz - 1 ? se[i + nxy] : c);
+                se[i] = (L.wx * sx + L.wy * sy + L.wz * sz - sr[i]) * inv;
+            }
+            __syncthreads();
+        }
+        part = 0.0f;
+        for (int i = threadIdx.x; i < n; i += kCoarseThreads) part += se[i];
+        const float mean_e = block_sum(part, red) / (float)n;
+        for (int i = threadIdx.x; i < n; i += kCoarseThreads) L.e[i] = se[i] - mean_e;
+        __syncthreads();
+    }
+}
+
+inline long long cdivl(long long a, long long b) { return (a + b - 1) / b; }
+
+constexpr int kFwd[3] = {0, 1, 2};  // aeroflux.go:373
+constexpr int kRev[3] = {2, 1, 0};  // aeroflux.go:390
+
+// Profile event slots.
+constexpr int kEvStart = 0, kEvEnd = 1, kEvSweep = 2 /* 2 per sweep */, kEvProj = 14 /* 2 per projection */;
+constexpr int kNumEvents = 18;
+
+// Device memory pool with first-fit placement and coalescing frees.
+struct Pool {
+    char* base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> bytes
+    bool init(size_t bytes) {
+        if (cudaMalloc(&base, bytes) != cudaSuccess) return false;
+        size = bytes;
+        free_[0] = bytes;
+        return true;
+    }
+    char* alloc(size_t bytes) {
+        bytes = (bytes + 255) & ~(size_t)255;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                const size_t off = it->first, rest = it->second - bytes;
+                free_.erase(it);
+                if (rest) free_[off + bytes] = rest;
+                return base + off;
+            }
+        }
+        return nullptr;
+    }
+    void release(char* p, size_t bytes) {
+        bytes = (bytes + 255) & ~(size_t)255;
+        size_t off = (size_t)(p - base);
+        auto next = free_.lower_bound(off);
+        if (next != free_.end() && off + bytes == next->first) {
+            bytes += next->second;
+            next = free_.erase(next);
+        }
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                prev->second += bytes;
+                return;
+            }
+        }
+        free_[off] = bytes;
+    }
+    size_t free_bytes() const {
+        size_t f = 0;
+        for (auto& kv : free_) f += kv.second;
+        return f;
+    }
+};
+
+struct SlotHost {
+    bool used = false;
+    bool active = false;
+    af_config cfg{};
+    InstDev d{};
+    af_field_desc desc[8]{};
+    char* mem = nullptr;   // pool or cudaMalloc block (arena unless external, b, multigrid)
+    size_t mem_bytes = 0;
+    bool external_arena = false;
+};
+
+}  // namespace
+
+struct Batch {
+    int cap = 0;
+    int sms = 152;
+    std::vector<SlotHost> slots;
+    Pool pool;
+    bool use_pool = false;
+    cudaStream_t stream = nullptr;
+    cudaStream_t body = nullptr;
+    InstDev* d_inst = nullptr;
+    Status* d_st = nullptr;
+    Ctl* d_ctl = nullptr;
+    int* d_tab = nullptr;            // S_COUNT prefix arrays of cap+1 ints
+    std::vector<int> h_tab;
+    Shape shape[S_COUNT];
+    int grid_sz[S_COUNT] = {};       // blocks per stage, fixed when the graph is captured
+    int graph_levels = 0;            // levels the captured graph covers
+    cudaGraphExec_t graph = nullptr;
+    bool tables_dirty = true;
+    bool profiling = false;
+    cudaEvent_t ev[kNumEvents] = {};
+    int64_t launches = 0;
+    int nu = 2;
+    int vcycles = 2;
+    int fixed_passes = 0;
+    cudaError_t capture_err = cudaSuccess;
+};
+
+namespace {
+
+int max_levels(const Batch* b) {
+    int m = 1;
+    for (const auto& s : b->slots)
+        if (s.used) m = std::max(m, s.d.nlev);
+    return m;
+}
+
+// Items of stage `st` for slot `s` under shape sh.
+long long stage_items(const SlotHost& S, int st, const Shape& sh) {
+    if (!S.used || !S.active) return 0;
+    const InstDev& I = S.d;
+    const long long per = (long long)sh.tpb * sh.ept;
+    long long n = 0;
+    if (st == S_BC) n = bc_count(I.g);
+    else if (st == S_SWEEP || st == S_GRAD) n = face_box(I.g);
+    else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
+    else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
+    else if (st == S_PBC) n = pbc_count(I.g);
+    else if (st == S_COARSE) return I.coarse_sweeps > 0 ? 1 : 0;
+    else if (st >= S_SMOOTH && st < S_RESTRICT) {
+        const int l = st - S_SMOOTH;
+        n = l < I.nlev - 1 ? half_box(I.lev[l]) : 0;
+    } else if (st >= S_RESTRICT && st < S_PROLONG) {
+        const int l = st - S_RESTRICT;
+        n = l < I.nlev - 1 ? lvl_cells(I.lev[l + 1]) : 0;
+    } else if (st >= S_PROLONG && st < S_BIGCOARSE) {
+        const int l = st - S_PROLONG;
+        n = l < I.nlev - 1 ? lvl_cells(I.lev[l]) : 0;
+    } else {
+        const int l = st - S_BIGCOARSE;
+        n = (l == I.nlev - 1 && I.coarse_sweeps == 0) ? half_box(I.lev[l]) : 0;
+    }
+    return cdivl(n, per);
+}
+
+cudaError_t upload_tables(Batch* b) {
+    const int w = b->cap + 1;
+    b->h_tab.assign((size_t)S_COUNT * w, 0);
+    for (int st = 0; st < S_COUNT; ++st) {
+        int* pre = &b->h_tab[(size_t)st * w];
+        long long acc = 0;
+        for (int s = 0; s < b->cap; ++s) {
+            pre[s] = (int)acc;
+            acc += stage_items(b->slots[s], st, b->shape[st]);
+        }
+        pre[b->cap] = (int)acc;
+    }
+    std::vector<InstDev> inst(b->cap);
+    for (int s = 0; s < b->cap; ++s) {
+        inst[s] = b->slots[s].d;
+        inst[s].active = b->slots[s].used && b->slots[s].active ? 1 : 0;
+    }
+    cudaError_t rc;
+    if ((rc = cudaMemcpyAsync(b->d_tab, b->h_tab.data(), b->h_tab.size() * sizeof(int), cudaMemcpyHostToDevice,
+                              b->stream)) != cudaSuccess)
+        return rc;
+    if ((rc = cudaMemcpyAsync(b->d_inst, inst.data(), inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
+                              b->stream)) != cudaSuccess)
+        return rc;
+    b->tables_dirty = false;
+    return cudaStreamSynchronize(b->stream);
+}
+
+Tab tab(const Batch* b, int st) { return Tab{b->d_tab + (size_t)st * (b->cap + 1), b->cap, b->shape[st].ept}; }
+int grid(const Batch* b, int st) { return b->grid_sz[st] > 0 ? b->grid_sz[st] : b->sms * b->shape[st].bpsm; }
+
+// Persistent grid of a stage: up to shape.bpsm blocks per SM, no more blocks
+// than tiles at capture time but at least one per SM, so slots assigned
+// later still spread over the whole GPU.
+void size_grids(Batch* b) {
+    const int w = b->cap + 1;
+    for (int st = 0; st < S_COUNT; ++st) {
+        const int items = b->h_tab[(size_t)st * w + b->cap];
+        b->grid_sz[st] = std::max(b->sms, std::min(items, b->sms * b->shape[st].bpsm));
+    }
+}
+
+#define LAUNCH(b, st, kernel, ...)                                                          \
+    do {                                                                                    \
+        kernel<<<grid(b, st), b->shape[st].tpb, 0, s>>>(__VA_ARGS__);                       \
+        ++b->launches;                                                                      \
+    } while (0)
+
+void rec(Batch* b, int idx, cudaStream_t s) {
+    if (b->profiling) cudaEventRecordWithFlags(b->ev[idx], s, cudaEventRecordExternal);
+}
+
+void enq_bc(Batch* b, int parity, int gate, cudaStream_t s) { LAUNCH(b, S_BC, kb_bc, b->d_inst, b->d_st, tab(b, S_BC), parity, gate); }
+
+void enq_sweep(Batch* b, int axis, int parity, int phase, cudaStream_t s) {
+    const Tab t = tab(b, S_SWEEP);
+    if (axis == 0) LAUNCH(b, S_SWEEP, kb_sweep<0>, b->d_inst, b->d_st, t, parity, phase);
+    else if (axis == 1) LAUNCH(b, S_SWEEP, kb_sweep<1>, b->d_inst, b->d_st, t, parity, phase);
+    else LAUNCH(b, S_SWEEP, kb_sweep<2>, b->d_inst, b->d_st, t, parity, phase);
+}
+
+void enq_smooth(Batch* b, int st, int l, int pairs, cudaStream_t s) {
+    for (int k = 0; k < pairs; ++k) {
+        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 0);
+        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 1);
+    }
+}
+
+void enq_vcycle(Batch* b, cudaStream_t s) {
+    const int L = b->graph_levels;
+    for (int l = 0; l + 1 < L; ++l) {
+        enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+        LAUNCH(b, S_RESTRICT + l, kb_restrict, b->d_inst, b->d_ctl, tab(b, S_RESTRICT + l), l);
+    }
+    LAUNCH(b, S_COARSE, kb_coarse, b->d_inst, b->d_ctl, tab(b, S_COARSE));
+    for (int l = 0; l < L; ++l) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, s);
+    for (int l = L - 2; l >= 0; --l) {
+        LAUNCH(b, S_PROLONG + l, kb_prolong, b->d_inst, b->d_ctl, tab(b, S_PROLONG + l), l);
+        enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+    }
+}
+
+void enq_pass(Batch* b, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int gate) {
+    for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, s);
+    LAUNCH(b, S_INT, kb_correct, b->d_inst, b->d_ctl, tab(b, S_INT));
+    LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 1);
+    kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate);
+    ++b->launches;
+}
+
+// project, project.go:12-34, with binary64 refinement; s must be capturing.
+void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
+    rec(b, kEvProj + (gate == 3 ? 0 : 2), s);
+    enq_bc(b, parity, gate, s);
+    LAUNCH(b, S_DIV, kb_div, b->d_inst, b->d_st, tab(b, S_DIV), parity, gate);
+    kb_init<<<1, 256, 0, s>>>(b->d_inst, b->d_ctl, b->cap);
+    ++b->launches;
+    LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 0);
+    if (b->fixed_passes > 0) {
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, 0, 0, 0, gate);
+        ++b->launches;
+        for (int k = 0; k < b->fixed_passes; ++k) enq_pass(b, s, 0, 0, gate);
+    } else {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t graph = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaError_t rc = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
+        if (rc != cudaSuccess || cs != cudaStreamCaptureStatusActive) {
+            b->capture_err = rc != cudaSuccess ? rc : cudaErrorStreamCaptureUnsupported;
+            return;
+        }
+        cudaGraphConditionalHandle h;
+        if ((rc = cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault)) != cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, 1, 0, gate);
+        ++b->launches;
+        if ((rc = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps)) != cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+        cudaGraphNodeParams params{cudaGraphNodeTypeConditional};
+        params.conditional.handle = h;
+        params.conditional.type = cudaGraphCondTypeWhile;
+        params.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((rc = cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &params)) != cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+        cudaGraph_t body = params.conditional.phGraph_out[0];
+        if ((rc = cudaStreamBeginCaptureToGraph(b->body, body, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+        enq_pass(b, b->body, h, 1, gate);
+        cudaGraph_t body_out = nullptr;
+        if ((rc = cudaStreamEndCapture(b->body, &body_out)) != cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+        if ((rc = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+            cudaSuccess) {
+            b->capture_err = rc;
+            return;
+        }
+    }
+    LAUNCH(b, S_PBC, kb_pbc, b->d_inst, b->d_st, tab(b, S_PBC), gate);
+    LAUNCH(b, S_GRAD, kb_grad, b->d_inst, b->d_st, tab(b, S_GRAD), parity, gate);
+    enq_bc(b, parity, gate, s);
+    rec(b, kEvProj + (gate == 3 ? 1 : 3), s);
+}
+
+// Step, aeroflux.go:348-409, for every active slot.
+void enq_step(Batch* b, cudaStream_t s) {
+    rec(b, kEvStart, s);
+    for (int k = 0; k < 6; ++k) {
+        const int axis = k < 3 ? kFwd[k] : kRev[k - 3];
+        enq_bc(b, k & 1, k, s);
+        rec(b, kEvSweep + 2 * k, s);
+        enq_sweep(b, axis, k & 1, k, s);
+        rec(b, kEvSweep + 2 * k + 1, s);
+        if (k == 2) enq_project(b, 1, 3, s);
+    }
+    enq_project(b, 0, 6, s);
+    kb_tick<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->cap);
+    ++b->launches;
+    rec(b, kEvEnd, s);
+}
+
+template <class F>
+cudaError_t capture(Batch* b, F body, cudaGraphExec_t* out) {
+    cudaGraph_t graph = nullptr;
+    cudaError_t rc = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (rc != cudaSuccess) return rc;
+    body();
+    rc = cudaStreamEndCapture(b->stream, &graph);
+    if (rc != cudaSuccess) return rc;
+    if (b->capture_err != cudaSuccess) {
+        rc = b->capture_err;
+        b->capture_err = cudaSuccess;
+        cudaGraphDestroy(graph);
+        return rc;
+    }
+    rc = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    return rc;
+}
+
+cudaError_t prepare(Batch* b) {
+    cudaError_t rc;
+    if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
+    const int L = max_levels(b);
+    if (b->graph && L > b->graph_levels) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!b->graph) {
+        b->graph_levels = std::max(L, b->graph_levels);
+        b->launches = 0;
+        size_grids(b);
+        if ((rc = capture(b, [&] { enq_step(b, b->stream); }, &b->graph)) != cudaSuccess) {
+            b->graph = nullptr;
+            return rc;
+        }
+    }
+    return cudaSuccess;
+}
+
+cudaError_t reset_status(Batch* b) {
+    std::vector<Status> h(b->cap, Status{kNoFault, 0u, kNoKey});
+    return cudaMemcpyAsync(b->d_st, h.data(), h.size() * sizeof(Status), cudaMemcpyHostToDevice, b->stream);
+}
+
+}  // namespace
+
+std::string fault_message_for(const Geom& g, unsigned gate, unsigned long long key);
+
+// ---------------------------------------------------------------------------
+// Host API
+// ---------------------------------------------------------------------------
+Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
+    Batch* b = new Batch();
+    b->cap = capacity;
+    b->slots.resize(capacity);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (const char* fp = getenv("AEROFLUX_FIXED_REFINEMENT_PASSES")) b->fixed_passes = std::max(0, atoi(fp));
+    // Shapes: the tiny per-slot control and coarse stages keep their own.
+    b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
+    cudaError_t rc;
+    if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_inst, sizeof(InstDev) * capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_st, sizeof(Status) * capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_ctl, sizeof(Ctl) * capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_tab, sizeof(int) * (size_t)S_COUNT * (capacity + 1))) != cudaSuccess) {
+        *err = std::string("aeroflux: batch tables: ") + cudaGetErrorString(rc);
+        batch_destroy(b);
+        return nullptr;
+    }
+    cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl) * capacity, b->stream);
+    if (pool_bytes) {
+        if (!b->pool.init(pool_bytes)) {
+            *err = "aeroflux: batch device pool of " + std::to_string(pool_bytes) + " bytes: out of memory";
+            batch_destroy(b);
+            return nullptr;
+        }
+        b->use_pool = true;
+    }
+    if (reset_status(b) != cudaSuccess || upload_tables(b) != cudaSuccess) {
+        *err = "aeroflux: batch setup failed";
+        batch_destroy(b);
+        return nullptr;
+    }
+    return b;
+}
+
+void batch_destroy(Batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& ev : b->ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto& s : b->slots)
+        if (s.used && !b->use_pool) cudaFree(s.mem);
+    if (b->use_pool) cudaFree(b->pool.base);
+    cudaFree(b->d_inst);
+    cudaFree(b->d_st);
+    cudaFree(b->d_ctl);
+    cudaFree(b->d_tab);
+    if (b->body) cudaStreamDestroy(b->body);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+namespace {
+
+// Multigrid hierarchy of a grid: coarsen every axis whose extent is even and
+// >= 4 until the grid has <= 64 cells or no axis halves.
+int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
+    int n = 0;
+    float wx = 1.0f, wy = 1.0f, wz = 1.0f;
+    while (true) {
+        Lvl& L = lev[n++];
+        L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr};
+        const long long c = (long long)nx * ny * nz;
+        const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
+        if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;
+        L.cx = cx;
+        L.cy = cy;
+        L.cz = cz;
+        if (cx) { nx /= 2; wx *= 0.25f; }
+        if (cy) { ny /= 2; wy *= 0.25f; }
+        if (cz) { nz /= 2; wz *= 0.25f; }
+    }
+    const Lvl& last = lev[n - 1];
+    if (lvl_cells(last) > kCoarseMax) {
+        *coarse_sweeps = 0;  // smoothing in place of a coarse solve
+    } else {
+        const int nmax = std::max(last.nx, std::max(last.ny, last.nz));
+        *coarse_sweeps = std::min(1000, std::max(8, 2 * nmax * nmax));
+    }
+    return n;
+}
+
+af_field_desc fdesc(int64_t* off, int64_t nx, int64_t ny, int64_t nz) {
+    af_field_desc f{*off, nx, ny, nz, nx, nx * ny, nx * ny * nz};
+    int64_t sz = f.count * 8;
+    if (int64_t r = sz % 128) sz += 128 - r;
+    *off += sz;
+    return f;
+}
+
+Dims dims_of(const af_field_desc& d) {
+    return Dims{(int)d.nx, (int)d.ny, (int)d.nz, d.sy, d.sz, d.count};
+}
+
+}  // namespace
+
+size_t batch_slot_bytes(const af_config& c) {
+    int64_t off = 0;
+    const int64_t g = c.ghost, cx = c.nx + 2 * g, cy = c.ny + 2 * g, cz = c.nz + 2 * g;
+    fdesc(&off, cx, cy, cz);
+    fdesc(&off, cx + 1, cy, cz);
+    fdesc(&off, cx, cy + 1, cz);
+    fdesc(&off, cx, cy, cz + 1);
+    fdesc(&off, cx, cy, cz);
+    fdesc(&off, cx + 1, cy, cz);
+    fdesc(&off, cx, cy + 1, cz);
+    fdesc(&off, cx, cy, cz + 1);
+    const size_t arena = ((size_t)off + 255) & ~(size_t)255;
+    const size_t bb = ((size_t)(cx * cy * cz) * 8 + 255) & ~(size_t)255;
+    Lvl lev[kMaxLev];
+    int cs = 0;
+    const int nl = plan_levels((int)c.nx, (int)c.ny, (int)c.nz, lev, &cs);
+    size_t mg = 0;
+    for (int l = 0; l < nl; ++l) mg += 2 * (size_t)lvl_cells(lev[l]) * sizeof(float);
+    return arena + bb + ((mg + 255) & ~(size_t)255);
+}
+
+int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
+    int s = -1;
+    for (int i = 0; i < b->cap; ++i)
+        if (!b->slots[i].used) {
+            s = i;
+            break;
+        }
+    if (s < 0) {
+        *err = "aeroflux: batch is full";
+        return -1;
+    }
+    SlotHost& S = b->slots[s];
+    S = SlotHost();
+    S.cfg = c;
+    InstDev& I = S.d;
+    // Layout, grid.go:101-134.
+    int64_t off = 0;
+    const int64_t g = c.ghost, cx = c.nx + 2 * g, cy = c.ny + 2 * g, cz = c.nz + 2 * g;
+    S.desc[0] = fdesc(&off, cx, cy, cz);
+    S.desc[1] = fdesc(&off, cx + 1, cy, cz);
+    S.desc[2] = fdesc(&off, cx, cy + 1, cz);
+    S.desc[3] = fdesc(&off, cx, cy, cz + 1);
+    S.desc[4] = fdesc(&off, cx, cy, cz);
+    S.desc[5] = fdesc(&off, cx + 1, cy, cz);
+    S.desc[6] = fdesc(&off, cx, cy + 1, cz);
+    S.desc[7] = fdesc(&off, cx, cy, cz + 1);
+    I.g.NX = (int)c.nx;
+    I.g.NY = (int)c.ny;
+    I.g.NZ = (int)c.nz;
+    I.g.G = (int)c.ghost;
+    I.g.p = dims_of(S.desc[0]);
+    I.g.u = dims_of(S.desc[1]);
+    I.g.v = dims_of(S.desc[2]);
+    I.g.w = dims_of(S.desc[3]);
+    I.nlev = plan_levels(I.g.NX, I.g.NY, I.g.NZ, I.lev, &I.coarse_sweeps);
+    const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
+    const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
+    size_t mg = 0;
+    for (int l = 0; l < I.nlev; ++l) mg += 2 * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
+    mg = (mg + 255) & ~(size_t)255;
+    S.external_arena = arena != nullptr;
+    S.mem_bytes = (arena ? 0 : arena_bytes) + b_bytes + mg;
+    if (b->use_pool) {
+        S.mem = b->pool.alloc(S.mem_bytes);
+        if (!S.mem) {
+            *err = "aeroflux: batch device pool exhausted";
+            S = SlotHost();
+            return -1;
+        }
+    } else if (cudaMalloc(&S.mem, S.mem_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *err = "aeroflux: batch slot allocation failed";
+        S = SlotHost();
+        return -1;
+    }
+    char* p = S.mem;
+    char* base = arena;
+    if (!arena) {
+        base = p;
+        p += arena_bytes;
+        cudaMemsetAsync(base, 0, arena_bytes, b->stream);  // MAC.Zero, grid.go:158-163
+    }
+    for (int f = 0; f < 8; ++f) I.slot[f] = (double*)(base + S.desc[f].off);
+    I.b = (double*)p;
+    p += b_bytes;
+    float* fp = (float*)p;
+    for (int l = 0; l < I.nlev; ++l) {
+        I.lev[l].e = fp;
+        I.lev[l].r = fp + lvl_cells(I.lev[l]);
+        fp += 2 * lvl_cells(I.lev[l]);
+    }
+    cudaMemsetAsync(p, 0, mg, b->stream);
+    const double half = c.dt * 0.5;  // aeroflux.go:353
+    const double invH = 1.0 / c.h;
+    I.dt_invh = (float)(half * invH);
+    I.lam = (float)(c.viscosity * half * invH * invH);  // stencil.go:73
+    I.div_scale = c.density / (c.dt * c.h);             // project.go:49
+    I.h2 = c.h * c.h;                                   // project.go:107
+    I.grad_scale = c.dt / (c.density * c.h);            // project.go:179
+    I.res_scale = c.dt / (c.density * c.h * c.h);
+    I.thresh = 0.5 * c.div_tol;
+    I.max_refine = (unsigned)c.max_refine;
+    I.parity = 0;
+    // Smoothing sweeps per level are a property of the batch's step graph:
+    // the first slot of an empty batch sets them.
+    bool empty = true;
+    for (int i = 0; i < b->cap; ++i)
+        if (i != s && b->slots[i].used) empty = false;
+    if (empty) b->nu = (int)c.inner_sweeps;
+    S.used = true;
+    S.active = true;
+    b->tables_dirty = true;
+    return s;
+}
+
+void batch_release(Batch* b, int s) {
+    SlotHost& S = b->slots[s];
+    if (!S.used) return;
+    cudaStreamSynchronize(b->stream);
+    if (b->use_pool) b->pool.release(S.mem, S.mem_bytes);
+    else cudaFree(S.mem);
+    S = SlotHost();
+    b->tables_dirty = true;
+}
+
+void batch_set_active(Batch* b, int s, bool active) {
+    if (b->slots[s].active != active) {
+        b->slots[s].active = active;
+        b->tables_dirty = true;
+    }
+}
+
+af_field_desc batch_field(const Batch* b, int s, int field, double** dev) {
+    const SlotHost& S = b->slots[s];
+    int f = field;
+    if (S.d.parity && field != 0 && field != 4) f = field <= 3 ? field + 4 : field - 4;
+    if (dev) *dev = S.d.slot[f];
+    return S.desc[f];
+}
+
+const Geom& batch_geom(const Batch* b, int s) { return b->slots[s].d.g; }
+cudaStream_t batch_stream(Batch* b) { return b->stream; }
+
+cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err) {
+    cudaError_t rc;
+    if ((rc = prepare(b)) != cudaSuccess) {
+        *err = std::string("aeroflux: cuda: preparing the batched step: ") + cudaGetErrorString(rc);
+        return rc;
+    }
+    if ((rc = reset_status(b)) != cudaSuccess) return rc;
+    for (int64_t i = 0; i < nsteps; ++i)
+        if ((rc = cudaGraphLaunch(b->graph, b->stream)) != cudaSuccess) {
+            *err = std::string("aeroflux: cuda: cudaGraphLaunch: ") + cudaGetErrorString(rc);
+            return rc;
+        }
+    return cudaSuccess;
+}
+
+cudaError_t batch_project(Batch* b, std::string* err) {
+    cudaError_t rc;
+    if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
+    if ((rc = reset_status(b)) != cudaSuccess) return rc;
+    if (max_levels(b) > b->graph_levels && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_levels = std::max(b->graph_levels, max_levels(b));
+    size_grids(b);
+    cudaGraphExec_t g = nullptr;
+    const bool prof = b->profiling;
+    b->profiling = false;
+    rc = capture(b, [&] { enq_project(b, 0, 0, b->stream); }, &g);
+    b->profiling = prof;
+    if (rc != cudaSuccess) {
+        *err = std::string("aeroflux: cuda: capturing the projection: ") + cudaGetErrorString(rc);
+        return rc;
+    }
+    rc = cudaGraphLaunch(g, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaGraphExecDestroy(g);
+    return rc;
+}
+
+cudaError_t batch_velocity_bc(Batch* b) {
+    cudaError_t rc;
+    if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
+    if ((rc = reset_status(b)) != cudaSuccess) return rc;
+    cudaStream_t s = b->stream;
+    enq_bc(b, 0, 0, s);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_sweep(Batch* b, int axis, double dt) {
+    cudaError_t rc;
+    // A sweep at a caller-chosen dt: the per-slot sweep constants change for
+    // this launch only.
+    std::vector<std::pair<float, float>> keep;
+    for (auto& S : b->slots) {
+        keep.emplace_back(S.d.dt_invh, S.d.lam);
+        if (!S.used) continue;
+        const double invH = 1.0 / S.cfg.h;
+        S.d.dt_invh = (float)(dt * invH);
+        S.d.lam = (float)(S.cfg.viscosity * dt * invH * invH);
+    }
+    if ((rc = upload_tables(b)) != cudaSuccess) return rc;
+    if ((rc = reset_status(b)) != cudaSuccess) return rc;
+    cudaStream_t s = b->stream;
+    enq_sweep(b, axis, 0, 0, s);
+    rc = cudaGetLastError();
+    for (int i = 0; i < b->cap; ++i) {
+        b->slots[i].d.dt_invh = keep[i].first;
+        b->slots[i].d.lam = keep[i].second;
+    }
+    b->tables_dirty = true;
+    if (rc != cudaSuccess) return rc;
+    if ((rc = cudaStreamSynchronize(s)) != cudaSuccess) return rc;
+    std::vector<Status> st(b->cap);
+    cudaMemcpy(st.data(), b->d_st, sizeof(Status) * b->cap, cudaMemcpyDeviceToHost);
+    for (int i = 0; i < b->cap; ++i)
+        if (b->slots[i].used && b->slots[i].active && st[i].fault_gate == kNoFault) b->slots[i].d.parity ^= 1;
+    b->tables_dirty = true;
+    return cudaSuccess;
+}
+
+int batch_collect_faults(Batch* b, std::string* msg, int* first_slot) {
+    std::vector<Status> st(b->cap);
+    cudaStreamSynchronize(b->stream);
+    cudaMemcpy(st.data(), b->d_st, sizeof(Status) * b->cap, cudaMemcpyDeviceToHost);
+    int n = 0;
+    *first_slot = -1;
+    for (int s = 0; s < b->cap; ++s) {
+        SlotHost& S = b->slots[s];
+        if (!S.used || st[s].fault_gate == kNoFault) continue;
+        if (n++ == 0) {
+            *first_slot = s;
+            *msg = fault_message_for(S.d.g, st[s].fault_gate, st[s].fault_key);
+        }
+        // The faulting step returned before commitVelocity of the faulting
+        // sweep: `phase` commits happened in it.
+        S.d.parity ^= (int)((st[s].fault_gate % 8u) & 1u);
+        b->tables_dirty = true;
+    }
+    return n;
+}
+
+bool batch_slot_faulted(const Batch* b, int s, std::string* msg) {
+    Status st;
+    cudaMemcpy(&st, b->d_st + s, sizeof st, cudaMemcpyDeviceToHost);
+    if (st.fault_gate == kNoFault) return false;
+    *msg = fault_message_for(b->slots[s].d.g, st.fault_gate, st.fault_key);
+    return true;
+}
+
+void batch_slot_projection(Batch* b, int s, int64_t* passes, double* max_div) {
+    Ctl c;
+    cudaStreamSynchronize(b->stream);
+    cudaMemcpy(&c, b->d_ctl + s, sizeof c, cudaMemcpyDeviceToHost);
+    *passes = c.passes;
+    *max_div = c.last_div;
+}
+
+cudaError_t batch_profile(Batch* b, bool on) {
+    if (on == b->profiling) return cudaSuccess;
+    cudaStreamSynchronize(b->stream);
+    if (on)
+        for (auto& ev : b->ev)
+            if (!ev) {
+                cudaError_t rc = cudaEventCreate(&ev);
+                if (rc != cudaSuccess) return rc;
+            }
+    b->profiling = on;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t batch_last_profile(Batch* b, double* step_ms, double* sweep_ms, double* proj_ms, int64_t* launches) {
+    if (!b->profiling) return cudaErrorInvalidValue;
+    cudaError_t rc = cudaStreamSynchronize(b->stream);
+    if (rc != cudaSuccess) return rc;
+    auto ms = [&](int a, int c) {
+        float t = 0;
+        rc = cudaEventElapsedTime(&t, b->ev[a], b->ev[c]);
+        return (double)t;
+    };
+    *step_ms = ms(kEvStart, kEvEnd);
+    *sweep_ms = 0;
+    for (int k = 0; k < 6; ++k) *sweep_ms += ms(kEvSweep + 2 * k, kEvSweep + 2 * k + 1);
+    *proj_ms = ms(kEvProj, kEvProj + 1) + ms(kEvProj + 2, kEvProj + 3);
+    *launches = b->launches;
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: for every stage that has work, time each candidate shape on the
+// current slots (each launch is idempotent or acts on scratch that the next
+// projection reinitialises; run it before uploading fields, or between
+// steps) and keep the fastest.
+// ---------------------------------------------------------------------------
+std::string batch_tune(Batch* b, int reps) {
+    const Shape cands[] = {{128, 1, 8}, {256, 1, 8}, {512, 1, 4}, {256, 2, 8}, {256, 4, 8},
+                           {128, 4, 16}, {256, 1, 16}, {512, 2, 4}, {1024, 1, 2}};
+    std::string report = "{";
+    for (int& gz : b->grid_sz) gz = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaStream_t s = b->stream;
+    kb_init<<<1, 256, 0, s>>>(b->d_inst, b->d_ctl, b->cap);
+    reset_status(b);
+    const int L = max_levels(b);
+    auto run = [&](int st) {
+        const Tab t = tab(b, st);
+        const int gsz = grid(b, st), tpb = b->shape[st].tpb;
+        if (st == S_BC) kb_bc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st == S_SWEEP) kb_sweep<0><<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st == S_DIV) kb_div<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st == S_INT) kb_residual<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, t, 0, 0);
+        else if (st == S_PBC) kb_pbc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0);
+        else if (st == S_GRAD) kb_grad<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st >= S_SMOOTH && st < S_RESTRICT) kb_smooth<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_SMOOTH, 0);
+        else if (st >= S_RESTRICT && st < S_PROLONG)
+            kb_restrict<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_RESTRICT);
+        else if (st >= S_PROLONG && st < S_BIGCOARSE)
+            kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG);
+    };
+    std::vector<int> stages = {S_BC, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD};
+    for (int l = 0; l + 1 < L; ++l) {
+        stages.push_back(S_SMOOTH + l);
+        stages.push_back(S_RESTRICT + l);
+        stages.push_back(S_PROLONG + l);
+    }
+    bool first = true;
+    for (int st : stages) {
+        long long items = 0;
+        for (auto& S : b->slots) items += stage_items(S, st, b->shape[st]);
+        if (!items) continue;
+        Shape best = b->shape[st];
+        float best_ms = 1e30f;
+        for (const Shape& c : cands) {
+            b->shape[st] = c;
+            upload_tables(b);
+            run(st);  // warm-up
+            cudaEventRecord(e0, s);
+            for (int r = 0; r < reps; ++r) run(st);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (cudaGetLastError() == cudaSuccess && ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+        b->shape[st] = best;
+        char buf[160];
+        snprintf(buf, sizeof buf, "%s\"stage_%d\": {\"tpb\": %d, \"ept\": %d, \"blocks_per_sm\": %d, \"us\": %.2f}",
+                 first ? "" : ", ", st, best.tpb, best.ept, best.bpsm, 1e3 * best_ms / reps);
+        report += buf;
+        first = false;
+    }
+    report += "}";
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    upload_tables(b);
+    kb_init<<<1, 256, 0, s>>>(b->d_inst, b->d_ctl, b->cap);
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaStreamSynchronize(s);
+    return report;
+}
+
+// Contained-fault text of the reference (arena.go:230-243 around Go's
+// bounds-check panic) for a NaN backtrace at fault key `key` in sweep phase
+// gate%8: the tap indices follow from the face, component, axis and strides.
+std::string fault_message_for(const Geom& g, unsigned gate, unsigned long long key) {
+    const int phase = (int)(gate % 8u);
+    const int axis = phase < 3 ? kFwd[phase] : kRev[phase - 3];
+    const int comp = (int)(key >> 60);
+    const unsigned long long z = (key >> 40) & 0xFFFFF, y = (key >> 20) & 0xFFFFF, x = key & 0xFFFFF;
+    const Dims& d = comp == 0 ? g.u : (comp == 1 ? g.v : g.w);
+    unsigned long long x0 = x, y0 = y, z0 = z;
+    const unsigned long long nan_int = 0x8000000000000000ull;
+    if (axis == 0) x0 = nan_int;
+    if (axis == 1) y0 = nan_int;
+    if (axis == 2) z0 = nan_int;
+    const unsigned long long sy = (unsigned long long)d.sy, sz = (unsigned long long)d.sz;
+    const unsigned long long i000 = x0 + y0 * sy + z0 * sz;
+    const unsigned long long taps[8] = {i000, i000 + 1, i000 + sy, i000 + sy + 1,
+                                        i000 + sz, i000 + sz + 1, i000 + sz + sy, i000 + sz + sy + 1};
+    char buf[200];
+    for (unsigned long long t : taps) {
+        const long long idx = (long long)t;
+        if (idx < 0) {
+            snprintf(buf, sizeof buf, "aeroflux: guard-page fault contained: runtime error: index out of range [%lld]", idx);
+            return buf;
+        }
+        if (idx >= d.count) {
+            snprintf(buf, sizeof buf,
+                     "aeroflux: guard-page fault contained: runtime error: index out of range [%lld] with length %lld",
+                     idx, (long long)d.count);
+            return buf;
+        }
+    }
+    return "aeroflux: guard-page fault contained: runtime error: index out of range";
+}
+
+}  // namespace af

@@ -1,0 +1,286 @@
+// af_cells.cuh -- per-cell device logic shared by the single-grid kernels
+// (af_fp64.cu) and the batched kernels (af_batch.cu), so both compute every
+// cell with the same instructions.  Internal to libaeroflux_cuda.
+#pragma once
+
+#include "af_internal.h"
+
+#include <math.h>
+
+namespace af {
+namespace cells {
+
+// --- exact binary64 (Go amd64 semantics: no contraction, RN) --------------
+constexpr unsigned long long kSign = 0x8000000000000000ull;
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+// Go's unary minus: a sign-bit flip (-0 for +0, payload kept for NaN).
+__device__ __forceinline__ double flip(double a) {
+    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(a) ^ kSign));
+}
+
+// Correctly rounded x/6.  Because 6 = 3*2, x/6 is never within ulp/6 of a
+// rounding midpoint, while q + r*c below is within 2^-54 ulp of x/6 (q =
+// RN(x*RN(1/6)), r = x - 6q computed exactly by the FMA, RN(1/6) = (1-2^-54)/6).
+// So RN(q + r*c) = RN(x/6).  This is the multiply-by-reciprocal-plus-remainder
+// division of Markstein (1990) / Brisebarre-Muller-Raina (2004), specialised
+// to divisor 6.  Outside the range where q and r stay normal (and for zero,
+// Inf, NaN) the IEEE division is used.  Three FP64 pipe operations instead of
+// a full reciprocal-refinement sequence.
+__device__ __forceinline__ double div6(double x) {
+    const double c = 0x1.5555555555555p-3;  // RN(1/6)
+    const double ax = fabs(x);
+    if (ax >= 0x1p-960 && ax < 0x1p1020) {
+        const double q = dmul(x, c);
+        const double r = __fma_rn(-6.0, q, x);
+        return __fma_rn(r, c, q);
+    }
+    return x / 6.0;
+}
+
+__device__ __forceinline__ bool gated(const Status* st, int gate) {
+    return st->fault_gate < st->step * 8u + (unsigned)gate;
+}
+
+// --- applyVelocityBC, stencil.go:246-315 ----------------------------------
+//
+// The reference writes the wall faces, then reflects tangential ghosts in a
+// fixed order where later passes read ghosts written by earlier ones (edges
+// and corners).  Composed, every written cell equals the sign-flipped value
+// of one interior cell: reflect each ghost coordinate into the interior,
+// flip the sign once per reflection, and read +0 where the source lies on a
+// wall face (zeroed by the first pass).  So every cell is written once from
+// cells nobody writes, and the reference's bits come out, -0 included.
+struct BcComp {
+    double* f;
+    long long s_n, s_1, s_2;  // strides along the normal axis and the two tangential axes
+    int Nn, N1, N2;           // interior extents along those axes
+};
+
+__device__ __forceinline__ long long bc_set_count(const BcComp& c, int set) {
+    return set == 0 ? 2ll * c.N1 * c.N2 : (set == 1 ? 2ll * (c.Nn + 1) * c.N2 : 2ll * (c.Nn + 1) * (c.N1 + 2));
+}
+
+__device__ __forceinline__ double bc_src(const BcComp& c, int G, int n, int a, int b) {
+    if (n == G || n == G + c.Nn) return 0.0;
+    return c.f[(long long)n * c.s_n + (long long)a * c.s_1 + (long long)b * c.s_2];
+}
+
+// Writes element i (< bc_set_count) of write set `set` of one component:
+// 0 = wall faces, 1 = ghosts of the first tangential axis, 2 = ghosts of the
+// second tangential axis (edges included).
+__device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long long i) {
+    int n, t1, t2;
+    double val;
+    if (set == 0) {
+        t1 = G + (int)(i % c.N1);
+        const long long r = i / c.N1;
+        t2 = G + (int)(r % c.N2);
+        n = (r / c.N2) ? G + c.Nn : G;
+        val = 0.0;
+    } else if (set == 1) {
+        n = G + (int)(i % (c.Nn + 1));
+        const long long r = i / (c.Nn + 1);
+        t2 = G + (int)(r % c.N2);
+        const int side = (int)(r / c.N2);
+        t1 = side ? G + c.N1 : G - 1;
+        const int s1 = side ? G + c.N1 - 1 : G;
+        val = flip(bc_src(c, G, n, s1, t2));
+    } else {
+        n = G + (int)(i % (c.Nn + 1));
+        const long long r = i / (c.Nn + 1);
+        t1 = G - 1 + (int)(r % (c.N1 + 2));
+        const int side = (int)(r / (c.N1 + 2));
+        t2 = side ? G + c.N2 : G - 1;
+        const int s2 = side ? G + c.N2 - 1 : G;
+        int s1 = t1;
+        bool odd = true;
+        if (t1 == G - 1) { s1 = G; odd = false; }
+        else if (t1 == G + c.N1) { s1 = G + c.N1 - 1; odd = false; }
+        const double s = bc_src(c, G, n, s1, s2);
+        val = odd ? flip(s) : s;
+    }
+    c.f[(long long)n * c.s_n + (long long)t1 * c.s_1 + (long long)t2 * c.s_2] = val;
+}
+
+__device__ __forceinline__ BcComp bc_comp(const Geom& g, int comp, double* u, double* v, double* w) {
+    if (comp == 0) return BcComp{u, 1, g.u.sy, g.u.sz, g.NX, g.NY, g.NZ};
+    if (comp == 1) return BcComp{v, g.v.sy, 1, g.v.sz, g.NY, g.NX, g.NZ};
+    return BcComp{w, g.w.sz, 1, g.w.sy, g.NZ, g.NX, g.NY};
+}
+
+// --- applyPressureBC, project.go:139-163 -----------------------------------
+// Composed, every first-layer ghost holds the interior cell at the clamped
+// coordinates.  Element i of set 0 (x ghosts), 1 (y ghosts), 2 (z ghosts).
+__device__ __forceinline__ long long pbc_set_count(const Geom& g, int set) {
+    return set == 0 ? 2ll * g.NY * g.NZ : (set == 1 ? 2ll * (g.NX + 2) * g.NZ : 2ll * (g.NX + 2) * (g.NY + 2));
+}
+
+__device__ __forceinline__ void pbc_cell(const Geom& g, double* p, int set, long long i) {
+    const int G = g.G, NX = g.NX, NY = g.NY, NZ = g.NZ;
+    int x, y, z;
+    if (set == 0) {
+        y = G + (int)(i % NY);
+        const long long r = i / NY;
+        z = G + (int)(r % NZ);
+        x = (r / NZ) ? G + NX : G - 1;
+    } else if (set == 1) {
+        x = G - 1 + (int)(i % (NX + 2));
+        const long long r = i / (NX + 2);
+        z = G + (int)(r % NZ);
+        y = (r / NZ) ? G + NY : G - 1;
+    } else {
+        x = G - 1 + (int)(i % (NX + 2));
+        const long long r = i / (NX + 2);
+        y = G - 1 + (int)(r % (NY + 2));
+        z = (r / (NY + 2)) ? G + NZ : G - 1;
+    }
+    const int cx = min(max(x, G), G + NX - 1);
+    const int cy = min(max(y, G), G + NY - 1);
+    const int cz = min(max(z, G), G + NZ - 1);
+    p[x + y * g.p.sy + z * g.p.sz] = p[cx + cy * g.p.sy + cz * g.p.sz];
+}
+
+// --- computeDivergence (project.go:42-62) + P zeroing + B = h2*Div ---------
+// (x, y, z) is any cell of the padded P extent.
+__device__ __forceinline__ void div_cell(const Geom& g, const double* __restrict__ u, const double* __restrict__ v,
+                                         const double* __restrict__ w, double* __restrict__ p,
+                                         double* __restrict__ dv, double* __restrict__ bb, double scale, double h2,
+                                         bool zero_p, int x, int y, int z) {
+    const long long i = x + y * g.p.sy + z * g.p.sz;
+    if (zero_p) p[i] = 0.0;
+    const int G = g.G;
+    if (x < G || x >= G + g.NX || y < G || y >= G + g.NY || z < G || z >= G + g.NZ) return;
+    const long long iu = x + y * g.u.sy + z * g.u.sz;
+    const long long iv = x + y * g.v.sy + z * g.v.sz;
+    const long long iw = x + y * g.w.sy + z * g.w.sz;
+    const double du = dsub(u[iu + 1], u[iu]);
+    const double dvv = dsub(v[iv + g.v.sy], v[iv]);
+    const double dw = dsub(w[iw + g.w.sz], w[iw]);
+    const double d = dmul(scale, dadd(dadd(du, dvv), dw));
+    dv[i] = d;
+    bb[i] = dmul(h2, d);
+}
+
+// --- subtractGradient, project.go:172-205 ----------------------------------
+// Face (x, y, z) of component c, inside that component's write range.
+__device__ __forceinline__ void grad_face(const Geom& g, const double* __restrict__ p, double* __restrict__ u,
+                                          double* __restrict__ v, double* __restrict__ w, double scale, int c, int x,
+                                          int y, int z) {
+    const long long ip = x + y * g.p.sy + z * g.p.sz;
+    if (c == 0) {
+        const long long i = x + y * g.u.sy + z * g.u.sz;
+        u[i] = dsub(u[i], dmul(scale, dsub(p[ip], p[ip - 1])));
+    } else if (c == 1) {
+        const long long i = x + y * g.v.sy + z * g.v.sz;
+        v[i] = dsub(v[i], dmul(scale, dsub(p[ip], p[ip - g.p.sy])));
+    } else {
+        const long long i = x + y * g.w.sy + z * g.w.sz;
+        w[i] = dsub(w[i], dmul(scale, dsub(p[ip], p[ip - g.p.sz])));
+    }
+}
+
+// --- binary64 <-> binary32 on the integer pipe -----------------------------
+// GB300 issues about two binary64 operations per SM per clock; these
+// conversions keep the mixed form off that pipe.
+
+// Round half away from zero on the magnitude; below FLT_MIN flushes to zero;
+// Inf/NaN kept.
+__device__ __forceinline__ float f64_to_f32(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FF);
+    if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u));
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sign);
+    if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);
+    const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rnd = (lo >> 28) & 1u;
+    return __uint_as_float(sign | (((unsigned)ef << 23) + mant + rnd));  // a carry rounds into the exponent
+}
+
+// Exact; subnormal floats flush to zero.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u;
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned mant = u & 0x7FFFFFu;
+    unsigned hi, lo = mant << 29;
+    if (e == 0) { hi = sign; lo = 0u; }
+    else if (e == 0xFF) hi = sign | 0x7FF00000u | (mant >> 3) | (mant ? 0x80000u : 0u);
+    else hi = sign | ((e - 127u + 1023u) << 20) | (mant >> 3);
+    return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+
+// --- binary32 advection + diffusion of one face (stencil.go:44-225) --------
+// Returns false on a NaN backtrace (a contained fault); the face is then not
+// written.  Only the active axis is interpolated: the other two weights are 0.
+template <int AX>
+__device__ __forceinline__ float mx_face_vel(const Geom& g, const double* u, const double* v, const double* w, int c,
+                                             int x, int y, int z) {
+    auto U = [&](int i, int j, int k) { return f64_to_f32(u[i + j * g.u.sy + k * g.u.sz]); };
+    auto V = [&](int i, int j, int k) { return f64_to_f32(v[i + j * g.v.sy + k * g.v.sz]); };
+    auto W = [&](int i, int j, int k) { return f64_to_f32(w[i + j * g.w.sy + k * g.w.sz]); };
+    if (c == 0) {
+        if (AX == 0) return U(x, y, z);
+        if (AX == 1) return 0.25f * (V(x - 1, y, z) + V(x, y, z) + V(x - 1, y + 1, z) + V(x, y + 1, z));
+        return 0.25f * (W(x - 1, y, z) + W(x, y, z) + W(x - 1, y, z + 1) + W(x, y, z + 1));
+    } else if (c == 1) {
+        if (AX == 0) return 0.25f * (U(x, y - 1, z) + U(x + 1, y - 1, z) + U(x, y, z) + U(x + 1, y, z));
+        if (AX == 1) return V(x, y, z);
+        return 0.25f * (W(x, y - 1, z) + W(x, y, z) + W(x, y - 1, z + 1) + W(x, y, z + 1));
+    } else {
+        if (AX == 0) return 0.25f * (U(x, y, z - 1) + U(x + 1, y, z - 1) + U(x, y, z) + U(x + 1, y, z));
+        if (AX == 1) return 0.25f * (V(x, y, z - 1) + V(x, y + 1, z - 1) + V(x, y, z) + V(x, y + 1, z));
+        return W(x, y, z);
+    }
+}
+
+template <int AX>
+__device__ __forceinline__ bool mx_sweep_face(const Geom& g, const double* u, const double* v, const double* w,
+                                              double* tu, double* tv, double* tw, float dt_invh, float lam, int c,
+                                              int x, int y, int z) {
+    const Dims& d = c == 0 ? g.u : (c == 1 ? g.v : g.w);
+    const double* sd = c == 0 ? u : (c == 1 ? v : w);
+    double* dd = c == 0 ? tu : (c == 1 ? tv : tw);
+    const float vel = mx_face_vel<AX>(g, u, v, w, c, x, y, z);
+    // Backtrace relative to the face, so binary32 keeps the fraction accurate
+    // at any grid size: departure = face + off, off = -dt*v/h.
+    const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+    const float off = -(vel * dt_invh);
+    if (isnan(off)) return false;
+    const float fl = floorf(off);
+    const float pos = (float)ca + off;
+    int i0;
+    float t;
+    if (!(pos > 0.0f)) {  // clamp into the padded field (stencil.go:174-188)
+        i0 = 0;
+        t = 0.0f;
+    } else if (pos >= (float)(na - 1)) {
+        i0 = na - 2;
+        t = 1.0f;
+    } else {
+        i0 = ca + (int)fl;
+        t = off - fl;
+        if (i0 >= na - 1) { i0 = na - 2; t = 1.0f; }
+    }
+    const long long s = AX == 0 ? 1 : (AX == 1 ? d.sy : d.sz);
+    const long long base = (long long)x + (long long)y * d.sy + (long long)z * d.sz;
+    const long long j0 = base + (long long)(i0 - ca) * s;
+    const float d0 = f64_to_f32(sd[j0]), d1 = f64_to_f32(sd[j0 + s]);
+    const float adv = fmaf(t, d1 - d0, d0);
+    float lap = 0.0f;
+    if (lam != 0.0f) {
+        const float c0 = f64_to_f32(sd[base]);
+        lap = lam * ((f64_to_f32(sd[base - s]) - 2.0f * c0) + f64_to_f32(sd[base + s]));
+    }
+    dd[base] = f32_to_f64(adv + lap);
+    return true;
+}
+
+}  // namespace cells
+}  // namespace af

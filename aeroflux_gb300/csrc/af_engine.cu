@@ -8,7 +8,7 @@
 // zero allocations per Step in the reference).
 #include "../../include/aeroflux_cuda.h"
 #include "af_internal.h"
-#include "af_mixed.h"
+#include "af_batch.h"
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -23,6 +23,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <vector>
 
 using af::Dims;
 using af::Fields;
@@ -199,7 +200,7 @@ struct af_engine {
     unsigned long long* mx = nullptr;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    af::MixedState* mixed = nullptr;
+    af::Batch* batch = nullptr;  // MIXED form: a batch of one over this arena
     // Profiling: event nodes at the step's ends, around each sweep and around
     // each projection's red-black loop.
     bool profiling = false;
@@ -210,6 +211,13 @@ struct af_engine {
     std::string err;
 
     double* slot(int id) const { return (double*)(arena + desc[id].off); }
+    // Current descriptor and device pointer of field id.
+    af_field_desc current(int id, double** dev) const {
+        if (batch) return af::batch_field(batch, 0, id, dev);
+        const int c = cur(id);
+        if (dev) *dev = slot(c);
+        return desc[c];
+    }
     // Current descriptor slot of field id (commitVelocity swaps U/V/W with Tmp0..2).
     int cur(int id) const {
         if (!parity) return id;
@@ -225,6 +233,17 @@ struct af_engine {
     }
     Fields fields() const {
         Fields f;
+        if (batch) {
+            af::batch_field(batch, 0, AF_FIELD_P, &f.p);
+            af::batch_field(batch, 0, AF_FIELD_U, &f.u);
+            af::batch_field(batch, 0, AF_FIELD_V, &f.v);
+            af::batch_field(batch, 0, AF_FIELD_W, &f.w);
+            af::batch_field(batch, 0, AF_FIELD_DIV, &f.div);
+            af::batch_field(batch, 0, AF_FIELD_TMP0, &f.t0);
+            af::batch_field(batch, 0, AF_FIELD_TMP1, &f.t1);
+            af::batch_field(batch, 0, AF_FIELD_TMP2, &f.t2);
+            return f;
+        }
         f.p = slot(AF_FIELD_P);
         f.u = slot(cur(AF_FIELD_U));
         f.v = slot(cur(AF_FIELD_V));
@@ -299,16 +318,7 @@ void enqueue_project_fp64(af_engine* e, const Fields& f, int gate) {
     af::launch_velocity_bc(g, f.u, f.v, f.w, e->st, gate, s);
 }
 
-void enqueue_project(af_engine* e, const Fields& f, int gate) {
-    if (e->mixed) {
-        // The profile's solve window spans the whole mixed projection.
-        rec(e, kEvRb + (gate == 3 ? 0 : 2));
-        af::enqueue_project_mixed(e->mixed, e->geom, e->cfg, f, e->st, gate, e->stream);
-        rec(e, kEvRb + (gate == 3 ? 1 : 3));
-    } else {
-        enqueue_project_fp64(e, f, gate);
-    }
-}
+void enqueue_project(af_engine* e, const Fields& f, int gate) { enqueue_project_fp64(e, f, gate); }
 
 void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {
     const Geom& g = e->geom;
@@ -316,8 +326,7 @@ void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {
     const double lam = e->cfg.viscosity * dt * invH * invH;  // stencil.go:73
     af::launch_velocity_bc(g, f.u, f.v, f.w, e->st, phase, e->stream);
     rec(e, kEvSweep + 2 * phase);
-    if (e->mixed) af::launch_sweep_mixed(e->mixed, g, axis, f, dt, invH, lam, e->st, phase, e->stream);
-    else af::launch_sweep_fp64(g, axis, f, dt, invH, lam, e->st, phase, e->stream);
+    af::launch_sweep_fp64(g, axis, f, dt, invH, lam, e->st, phase, e->stream);
     rec(e, kEvSweep + 2 * phase + 1);
     e->launches_per_step += 2;
     swap_fields(f);  // commitVelocity, stencil.go:230-235
@@ -346,13 +355,6 @@ int capture(af_engine* e, F body, cudaGraphExec_t* out) {
     body();
     cudaError_t rc = cudaStreamEndCapture(e->stream, &graph);
     if (rc != cudaSuccess) return cuda_fail(e, rc, "cudaStreamEndCapture");
-    if (e->mixed) {
-        cudaError_t mrc = af::mixed_capture_error(e->mixed);
-        if (mrc != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            return cuda_fail(e, mrc, "capturing the refinement loop");
-        }
-    }
     rc = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (rc != cudaSuccess) return cuda_fail(e, rc, "cudaGraphInstantiate");
@@ -361,34 +363,8 @@ int capture(af_engine* e, F body, cudaGraphExec_t* out) {
 
 int build_graph(af_engine* e) { return capture(e, [&] { enqueue_step(e); }, &e->graph[e->parity]); }
 
-// Rebuilds the reference's contained-fault text from a fault key: the fault
-// only fires on a NaN backtrace coordinate, so the tap indices follow from
-// the face, the component, the axis and the source field's strides alone.
 std::string fault_message(const af_engine* e, unsigned gate, unsigned long long key) {
-    const int phase = (int)(gate % 8u);
-    const int axis = phase < 3 ? kFwd[phase] : kRev[phase - 3];
-    const int comp = (int)(key >> 60);
-    const long long z = (long long)((key >> 40) & 0xFFFFF), y = (long long)((key >> 20) & 0xFFFFF),
-                    x = (long long)(key & 0xFFFFF);
-    const af_field_desc& d = e->desc[AF_FIELD_U + comp];
-    unsigned long long x0 = (unsigned long long)x, y0 = (unsigned long long)y, z0 = (unsigned long long)z;
-    const unsigned long long nan_int = 0x8000000000000000ull;
-    if (axis == 0) x0 = nan_int;
-    if (axis == 1) y0 = nan_int;
-    if (axis == 2) z0 = nan_int;
-    const unsigned long long sy = (unsigned long long)d.sy, sz = (unsigned long long)d.sz;
-    const unsigned long long i000 = x0 + y0 * sy + z0 * sz;
-    const unsigned long long taps[8] = {i000, i000 + 1, i000 + sy, i000 + sy + 1,
-                                        i000 + sz, i000 + sz + 1, i000 + sz + sy, i000 + sz + sy + 1};
-    for (unsigned long long t : taps) {
-        const long long idx = (long long)t;
-        if (idx < 0)
-            return sfmt("aeroflux: guard-page fault contained: runtime error: index out of range [%lld]", idx);
-        if (idx >= d.count)
-            return sfmt("aeroflux: guard-page fault contained: runtime error: index out of range [%lld] with length %lld",
-                        idx, (long long)d.count);
-    }
-    return "aeroflux: guard-page fault contained: runtime error: index out of range";
+    return af::fault_message_for(e->geom, gate, key);
 }
 
 void drop_graphs(af_engine* e) {
@@ -400,7 +376,7 @@ int release(af_engine* e) {
     drop_graphs(e);
     for (auto& ev : e->ev)
         if (ev) { cudaEventDestroy(ev); ev = nullptr; }
-    if (e->mixed) { af::mixed_destroy(e->mixed); e->mixed = nullptr; }
+    if (e->batch) { af::batch_destroy(e->batch); e->batch = nullptr; }
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->arena);
     cudaFree(e->b);
@@ -414,6 +390,22 @@ int release(af_engine* e) {
     e->partials = e->sum = nullptr;
     e->mx = nullptr;
     if (e->stream) { cudaStreamDestroy(e->stream); e->stream = nullptr; }
+    return AF_OK;
+}
+
+// MIXED: wait for the batch stream and turn a slot fault into the error.
+int batch_check(af_engine* e, cudaError_t rc, const std::string& what) {
+    if (rc != cudaSuccess) {
+        e->err = what.empty() ? sfmt("aeroflux: cuda: %s", cudaGetErrorString(rc)) : what;
+        return AF_ERR_CUDA;
+    }
+    if ((rc = cudaStreamSynchronize(af::batch_stream(e->batch))) != cudaSuccess) return cuda_fail(e, rc, "batch");
+    std::string msg;
+    int first = -1;
+    if (af::batch_collect_faults(e->batch, &msg, &first)) {
+        e->err = msg;
+        return AF_ERR_FAULT;
+    }
     return AF_OK;
 }
 
@@ -518,9 +510,11 @@ int af_create(const af_config* cin, af_engine** out, char* err, size_t errlen) {
     if ((cr = cudaMemsetAsync(e->arena, 0, (size_t)e->bytes, e->stream)) != cudaSuccess)
         return (cuda_fail(e, cr, "cudaMemset"), fail(AF_ERR_CUDA));
     if (c.precision == AF_PRECISION_MIXED) {
+        if ((cr = cudaStreamSynchronize(e->stream)) != cudaSuccess)
+            return (cuda_fail(e, cr, "cudaStreamSynchronize"), fail(AF_ERR_CUDA));
         std::string merr;
-        e->mixed = af::mixed_create(g, c, e->stream, &merr);
-        if (!e->mixed) {
+        e->batch = af::batch_create(1, 0, &merr);
+        if (!e->batch || af::batch_assign(e->batch, c, e->arena, &merr) != 0) {
             e->err = merr;
             return fail(AF_ERR_NOMEM);
         }
@@ -540,7 +534,7 @@ int af_get_config(const af_engine* e, af_config* out) {
 
 int af_field_info(const af_engine* e, int field, af_field_desc* out) {
     if (!e || !out || field < 0 || field > 7) return AF_ERR_ARG;
-    *out = e->desc[e->cur(field)];
+    *out = e->current(field, nullptr);
     return AF_OK;
 }
 
@@ -550,12 +544,13 @@ int af_field_upload(af_engine* e, int field, const double* host, size_t count) {
         e->err = "aeroflux: bad field upload arguments";
         return AF_ERR_ARG;
     }
-    const af_field_desc& d = e->desc[e->cur(field)];
+    double* dev = nullptr;
+    const af_field_desc d = e->current(field, &dev);
     if ((int64_t)count != d.count) {
         e->err = sfmt("aeroflux: field upload of %lld values, field holds %lld", (long long)count, (long long)d.count);
         return AF_ERR_ARG;
     }
-    AF_CUDA(e, cudaMemcpyAsync(e->arena + d.off, host, count * 8, cudaMemcpyHostToDevice, e->stream));
+    AF_CUDA(e, cudaMemcpyAsync(dev, host, count * 8, cudaMemcpyHostToDevice, e->stream));
     AF_CUDA(e, cudaStreamSynchronize(e->stream));
     return AF_OK;
 }
@@ -566,19 +561,21 @@ int af_field_download(af_engine* e, int field, double* host, size_t count) {
         e->err = "aeroflux: bad field download arguments";
         return AF_ERR_ARG;
     }
-    const af_field_desc& d = e->desc[e->cur(field)];
+    double* dev = nullptr;
+    const af_field_desc d = e->current(field, &dev);
     if ((int64_t)count != d.count) {
         e->err = sfmt("aeroflux: field download of %lld values, field holds %lld", (long long)count,
                       (long long)d.count);
         return AF_ERR_ARG;
     }
-    AF_CUDA(e, cudaMemcpyAsync(host, e->arena + d.off, count * 8, cudaMemcpyDeviceToHost, e->stream));
+    AF_CUDA(e, cudaMemcpyAsync(host, dev, count * 8, cudaMemcpyDeviceToHost, e->stream));
     AF_CUDA(e, cudaStreamSynchronize(e->stream));
     return AF_OK;
 }
 
 int af_apply_velocity_bc(af_engine* e) {
     if (int rc = check_open(e)) return rc;
+    if (e->batch) return batch_check(e, af::batch_velocity_bc(e->batch), "");
     if (int rc = reset_status(e)) return rc;
     Fields f = e->fields();
     af::launch_velocity_bc(e->geom, f.u, f.v, f.w, e->st, 0, e->stream);
@@ -593,6 +590,11 @@ int af_step(af_engine* e, int64_t nsteps) {
         return AF_ERR_ARG;
     }
     if (nsteps == 0) return AF_OK;
+    if (e->batch) {
+        std::string err;
+        cudaError_t rc = af::batch_step(e->batch, nsteps, &err);
+        return batch_check(e, rc, err);
+    }
     if (!e->graph[e->parity])
         if (int rc = build_graph(e)) return rc;
     if (int rc = reset_status(e)) return rc;
@@ -602,18 +604,13 @@ int af_step(af_engine* e, int64_t nsteps) {
 
 int af_project(af_engine* e) {
     if (int rc = check_open(e)) return rc;
-    if (int rc = reset_status(e)) return rc;
-    if (e->mixed) {
-        // The refinement loop is a graph node: run the projection as a graph.
-        cudaGraphExec_t g = nullptr;
-        if (int rc = capture(e, [&] { enqueue_project(e, e->fields(), 0); }, &g)) return rc;
-        cudaError_t lrc = cudaGraphLaunch(g, e->stream);
-        cudaStreamSynchronize(e->stream);
-        cudaGraphExecDestroy(g);
-        if (lrc != cudaSuccess) return cuda_fail(e, lrc, "cudaGraphLaunch");
-    } else {
-        enqueue_project(e, e->fields(), 0);
+    if (e->batch) {
+        std::string err;
+        cudaError_t rc = af::batch_project(e->batch, &err);
+        return batch_check(e, rc, err);
     }
+    if (int rc = reset_status(e)) return rc;
+    enqueue_project(e, e->fields(), 0);
     AF_CUDA(e, cudaGetLastError());
     return sync_and_check(e);
 }
@@ -624,12 +621,12 @@ int af_phase_sweep(af_engine* e, int axis, double dt) {
         e->err = "aeroflux: axis must be 0, 1 or 2";
         return AF_ERR_ARG;
     }
+    if (e->batch) return batch_check(e, af::batch_sweep(e->batch, axis, dt), "");
     if (int rc = reset_status(e)) return rc;
     Fields f = e->fields();
     const double invH = 1.0 / e->cfg.h;
     const double lam = e->cfg.viscosity * dt * invH * invH;
-    if (e->mixed) af::launch_sweep_mixed(e->mixed, e->geom, axis, f, dt, invH, lam, e->st, 0, e->stream);
-    else af::launch_sweep_fp64(e->geom, axis, f, dt, invH, lam, e->st, 0, e->stream);
+    af::launch_sweep_fp64(e->geom, axis, f, dt, invH, lam, e->st, 0, e->stream);
     AF_CUDA(e, cudaGetLastError());
     Status s;
     AF_CUDA(e, cudaMemcpyAsync(&s, e->st, sizeof s, cudaMemcpyDeviceToHost, e->stream));
@@ -645,7 +642,7 @@ int af_phase_sweep(af_engine* e, int axis, double dt) {
 
 int af_phase_divergence(af_engine* e) {
     if (int rc = check_open(e)) return rc;
-    if (e->mixed) {
+    if (e->batch) {
         e->err = "aeroflux: phase hooks of the projection exist for the FP64 form only";
         return AF_ERR_UNSUPPORTED;
     }
@@ -659,7 +656,7 @@ int af_phase_divergence(af_engine* e) {
 
 int af_phase_red_black(af_engine* e) {
     if (int rc = check_open(e)) return rc;
-    if (e->mixed) {
+    if (e->batch) {
         e->err = "aeroflux: phase hooks of the projection exist for the FP64 form only";
         return AF_ERR_UNSUPPORTED;
     }
@@ -757,17 +754,20 @@ int af_enable_sparse_solver(af_engine* e) {
 int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div) {
     if (int rc = check_open(e)) return rc;
     if (!passes || !max_div) return AF_ERR_ARG;
-    if (!e->mixed) {
+    if (!e->batch) {
         *passes = 0;
         return af_max_divergence(e, max_div);
     }
-    AF_CUDA(e, cudaStreamSynchronize(e->stream));
-    af::mixed_stats(e->mixed, passes, max_div);
+    af::batch_slot_projection(e->batch, 0, passes, max_div);
     return AF_OK;
 }
 
 int af_profile(af_engine* e, int enable) {
     if (int rc = check_open(e)) return rc;
+    if (e->batch) {
+        AF_CUDA(e, af::batch_profile(e->batch, enable != 0));
+        return AF_OK;
+    }
     const bool on = enable != 0;
     if (on == e->profiling) return AF_OK;
     AF_CUDA(e, cudaStreamSynchronize(e->stream));
@@ -782,6 +782,12 @@ int af_profile(af_engine* e, int enable) {
 int af_last_step_profile(af_engine* e, af_step_profile* out) {
     if (int rc = check_open(e)) return rc;
     if (!out) return AF_ERR_ARG;
+    if (e->batch) {
+        af_step_profile p{};
+        AF_CUDA(e, af::batch_last_profile(e->batch, &p.step_ms, &p.sweep_ms, &p.rbgs_ms, &p.kernel_launches));
+        *out = p;
+        return AF_OK;
+    }
     if (!e->profiling || !e->graph[e->parity]) {
         e->err = "aeroflux: profiling is off or no step has run";
         return AF_ERR_ARG;
@@ -825,5 +831,223 @@ void af_destroy(af_engine* e) {
 }
 
 const char* af_last_error(const af_engine* e) { return e ? e->err.c_str() : ""; }
+
+// ---------------------------------------------------------------------------
+// Batched form
+// ---------------------------------------------------------------------------
+struct af_batch {
+    af::Batch* b = nullptr;
+    int device = 0;
+    unsigned long long* mx = nullptr;  // MaxDivergence result word
+    std::vector<af_config> cfg;
+    std::string err;
+};
+
+namespace {
+
+int batch_fail(af_batch* h, int code, const std::string& m) {
+    h->err = m;
+    return code;
+}
+
+int batch_slot_ok(const af_batch* h, int64_t slot) {
+    return h && slot >= 0 && slot < (int64_t)h->cfg.size() && h->cfg[slot].nx > 0;
+}
+
+int batch_wait(af_batch* h) {
+    cudaError_t rc = cudaStreamSynchronize(af::batch_stream(h->b));
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, sfmt("aeroflux: cuda: %s", cudaGetErrorString(rc)));
+    return AF_OK;
+}
+
+}  // namespace
+
+int af_batch_create(int64_t capacity, int64_t pool_bytes, int32_t device, af_batch** out, char* err, size_t errlen) {
+    if (!out || capacity < 1 || pool_bytes < 0 || device < 0) return AF_ERR_ARG;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        put_err(err, errlen, "aeroflux: cuda: no such device");
+        return AF_ERR_CUDA;
+    }
+    std::string m;
+    af::Batch* b = af::batch_create((int)capacity, (size_t)pool_bytes, &m);
+    if (!b) {
+        put_err(err, errlen, m);
+        return AF_ERR_NOMEM;
+    }
+    af_batch* h = new af_batch();
+    h->b = b;
+    h->device = device;
+    if (cudaMalloc(&h->mx, sizeof *h->mx) != cudaSuccess) {
+        af::batch_destroy(b);
+        delete h;
+        put_err(err, errlen, "aeroflux: cuda: batch result word");
+        return AF_ERR_NOMEM;
+    }
+    h->cfg.assign((size_t)capacity, af_config{});
+    *out = h;
+    return AF_OK;
+}
+
+int af_batch_slot_bytes(const af_config* cfg, int64_t* bytes) {
+    if (!cfg || !bytes) return AF_ERR_ARG;
+    af_config c = *cfg;
+    if (!normalize(&c).empty()) return AF_ERR_CONFIG;
+    *bytes = (int64_t)af::batch_slot_bytes(c);
+    return AF_OK;
+}
+
+int af_batch_assign(af_batch* h, const af_config* cfg, int64_t* slot) {
+    if (!h || !cfg || !slot) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    af_config c = *cfg;
+    std::string m = normalize(&c);
+    if (!m.empty()) return batch_fail(h, AF_ERR_CONFIG, m);
+    if (c.precision != AF_PRECISION_MIXED)
+        return batch_fail(h, AF_ERR_CONFIG, "aeroflux: batches step the mixed-precision form only");
+    const int s = af::batch_assign(h->b, c, nullptr, &m);
+    if (s < 0) return batch_fail(h, AF_ERR_NOMEM, m);
+    h->cfg[s] = c;
+    *slot = s;
+    return batch_wait(h);
+}
+
+int af_batch_release(af_batch* h, int64_t slot) {
+    if (!batch_slot_ok(h, slot)) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    af::batch_release(h->b, (int)slot);
+    h->cfg[slot] = af_config{};
+    return AF_OK;
+}
+
+int af_batch_set_active(af_batch* h, int64_t slot, int active) {
+    if (!batch_slot_ok(h, slot)) return AF_ERR_ARG;
+    af::batch_set_active(h->b, (int)slot, active != 0);
+    return AF_OK;
+}
+
+int af_batch_get_config(const af_batch* h, int64_t slot, af_config* out) {
+    if (!batch_slot_ok(h, slot) || !out) return AF_ERR_ARG;
+    *out = h->cfg[slot];
+    return AF_OK;
+}
+
+int af_batch_field_info(const af_batch* h, int64_t slot, int field, af_field_desc* out) {
+    if (!batch_slot_ok(h, slot) || !out || field < 0 || field > 7) return AF_ERR_ARG;
+    *out = af::batch_field(h->b, (int)slot, field, nullptr);
+    return AF_OK;
+}
+
+static int batch_copy(af_batch* h, int64_t slot, int field, void* host, size_t count, bool up) {
+    if (!batch_slot_ok(h, slot) || !host || field < 0 || field > 7) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    double* dev = nullptr;
+    const af_field_desc d = af::batch_field(h->b, (int)slot, field, &dev);
+    if ((int64_t)count != d.count)
+        return batch_fail(h, AF_ERR_ARG, sfmt("aeroflux: field copy of %lld values, field holds %lld",
+                                              (long long)count, (long long)d.count));
+    cudaStream_t s = af::batch_stream(h->b);
+    cudaError_t rc = up ? cudaMemcpyAsync(dev, host, count * 8, cudaMemcpyHostToDevice, s)
+                        : cudaMemcpyAsync(host, dev, count * 8, cudaMemcpyDeviceToHost, s);
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, sfmt("aeroflux: cuda: %s", cudaGetErrorString(rc)));
+    return batch_wait(h);
+}
+
+int af_batch_field_upload(af_batch* h, int64_t slot, int field, const double* host, size_t count) {
+    return batch_copy(h, slot, field, const_cast<double*>(host), count, true);
+}
+
+int af_batch_field_download(af_batch* h, int64_t slot, int field, double* host, size_t count) {
+    return batch_copy(h, slot, field, host, count, false);
+}
+
+int af_batch_apply_velocity_bc(af_batch* h) {
+    if (!h) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    cudaError_t rc = af::batch_velocity_bc(h->b);
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, sfmt("aeroflux: cuda: %s", cudaGetErrorString(rc)));
+    return batch_wait(h);
+}
+
+int af_batch_step(af_batch* h, int64_t nsteps) {
+    if (!h || nsteps < 0) return AF_ERR_ARG;
+    if (nsteps == 0) return AF_OK;
+    cudaSetDevice(h->device);
+    std::string m;
+    cudaError_t rc = af::batch_step(h->b, nsteps, &m);
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, m);
+    if (int r = batch_wait(h)) return r;
+    int first = -1;
+    af::batch_collect_faults(h->b, &m, &first);
+    return AF_OK;
+}
+
+int af_batch_slot_status(af_batch* h, int64_t slot, int32_t* faulted, char* msg, size_t msglen) {
+    if (!batch_slot_ok(h, slot) || !faulted) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    std::string m;
+    *faulted = af::batch_slot_faulted(h->b, (int)slot, &m) ? 1 : 0;
+    put_err(msg, msglen, *faulted ? m : "");
+    return AF_OK;
+}
+
+int af_batch_max_divergence(af_batch* h, int64_t slot, double* out) {
+    if (!batch_slot_ok(h, slot) || !out) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    double *u, *v, *w;
+    af::batch_field(h->b, (int)slot, AF_FIELD_U, &u);
+    af::batch_field(h->b, (int)slot, AF_FIELD_V, &v);
+    af::batch_field(h->b, (int)slot, AF_FIELD_W, &w);
+    cudaStream_t s = af::batch_stream(h->b);
+    cudaMemsetAsync(h->mx, 0, sizeof *h->mx, s);
+    af::launch_max_divergence(af::batch_geom(h->b, (int)slot), u, v, w, 1.0 / h->cfg[slot].h, h->mx, s);
+    unsigned long long bits = 0;
+    cudaMemcpyAsync(&bits, h->mx, sizeof bits, cudaMemcpyDeviceToHost, s);
+    if (int r = batch_wait(h)) return r;
+    memcpy(out, &bits, sizeof bits);
+    return AF_OK;
+}
+
+int af_batch_projection_stats(af_batch* h, int64_t slot, int64_t* passes, double* max_div) {
+    if (!batch_slot_ok(h, slot) || !passes || !max_div) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    af::batch_slot_projection(h->b, (int)slot, passes, max_div);
+    return AF_OK;
+}
+
+int af_batch_tune(af_batch* h, int32_t reps, char* report, size_t len) {
+    if (!h || reps < 1) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    const std::string r = af::batch_tune(h->b, reps);
+    put_err(report, len, r);
+    return AF_OK;
+}
+
+int af_batch_profile(af_batch* h, int enable) {
+    if (!h) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    cudaError_t rc = af::batch_profile(h->b, enable != 0);
+    return rc == cudaSuccess ? AF_OK : batch_fail(h, AF_ERR_CUDA, cudaGetErrorString(rc));
+}
+
+int af_batch_last_step_profile(af_batch* h, af_step_profile* out) {
+    if (!h || !out) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    af_step_profile p{};
+    cudaError_t rc = af::batch_last_profile(h->b, &p.step_ms, &p.sweep_ms, &p.rbgs_ms, &p.kernel_launches);
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, "aeroflux: profiling is off or no step has run");
+    *out = p;
+    return AF_OK;
+}
+
+void af_batch_destroy(af_batch* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    af::batch_destroy(h->b);
+    cudaFree(h->mx);
+    delete h;
+}
+
+const char* af_batch_last_error(const af_batch* h) { return h ? h->err.c_str() : ""; }
 
 }  // extern "C"

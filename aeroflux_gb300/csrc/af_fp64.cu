@@ -9,6 +9,7 @@
 // kernel boundary.  Every stage is per-cell independent, so results do not
 // depend on the launch shape.
 #include "../../include/aeroflux_cuda.h"
+#include "af_cells.cuh"
 #include "af_internal.h"
 
 #include <math.h>
@@ -21,102 +22,17 @@
 namespace af {
 namespace {
 
-constexpr unsigned long long kSign = 0x8000000000000000ull;
+using namespace cells;
 
-__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double flip(double a) {
-    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(a) ^ kSign));
-}
-
-// Correctly rounded x/6.  Because 6 = 3*2, x/6 is never within ulp/6 of a
-// rounding midpoint, while q + r*c below is within 2^-54 ulp of x/6 (q =
-// RN(x*RN(1/6)), r = x - 6q computed exactly by the FMA, RN(1/6) = (1-2^-54)/6).
-// So RN(q + r*c) = RN(x/6).  This is the multiply-by-reciprocal-plus-remainder
-// division of Markstein (1990) / Brisebarre-Muller-Raina (2004), specialised
-// to divisor 6.  Outside the range where q and r stay normal (and for zero,
-// Inf, NaN) the IEEE division is used.  Three FP64 pipe operations instead of
-// a full reciprocal-refinement sequence.
-__device__ __forceinline__ double div6(double x) {
-    const double c = 0x1.5555555555555p-3;  // RN(1/6)
-    const double ax = fabs(x);
-    if (ax >= 0x1p-960 && ax < 0x1p1020) {
-        const double q = dmul(x, c);
-        const double r = __fma_rn(-6.0, q, x);
-        return __fma_rn(r, c, q);
-    }
-    return x / 6.0;
-}
-
-__device__ __forceinline__ bool gated(const Status* st, int gate) {
-    return st->fault_gate < st->step * 8u + (unsigned)gate;
-}
-
-// ---------------------------------------------------------------------------
-// applyVelocityBC, stencil.go:246-315.
-//
-// The reference writes the wall faces, then reflects tangential ghosts in a
-// fixed order where later passes read ghosts written by earlier ones (edges
-// and corners).  Composed, every written cell equals the sign-flipped value
-// of one interior cell: reflect each ghost coordinate into the interior,
-// flip the sign once per reflection, and read +0 where the source lies on a
-// wall face (zeroed by the first pass).  So one kernel writes each cell once
-// from unwritten cells only, and produces the reference's bits, -0 included.
-// ---------------------------------------------------------------------------
-struct BcComp {
-    double* f;
-    long long s_n, s_1, s_2;  // strides along the normal axis and the two tangential axes
-    int Nn, N1, N2;           // interior extents along those axes
-};
-
-__device__ __forceinline__ double bc_src(const BcComp& c, int G, int n, int a, int b) {
-    if (n == G || n == G + c.Nn) return 0.0;
-    return c.f[(long long)n * c.s_n + (long long)a * c.s_1 + (long long)b * c.s_2];
-}
-
-__global__ void k_velocity_bc(BcComp cu, BcComp cv, BcComp cw, int G, Status* st, int gate) {
+// applyVelocityBC, stencil.go:246-315: 3 components x 3 write sets, each cell
+// written once (see bc_cell).
+__global__ void k_velocity_bc(Geom g, double* u, double* v, double* w, Status* st, int gate) {
     if (gated(st, gate)) return;
     const int comp = blockIdx.y / 3, set = blockIdx.y % 3;
-    const BcComp& c = comp == 0 ? cu : (comp == 1 ? cv : cw);
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int n, t1, t2;
-    double val;
-    if (set == 0) {  // wall faces: +0
-        const long long cnt = 2ll * c.N1 * c.N2;
-        if (i >= cnt) return;
-        t1 = G + (int)(i % c.N1);
-        long long r = i / c.N1;
-        t2 = G + (int)(r % c.N2);
-        n = (r / c.N2) ? G + c.Nn : G;
-        val = 0.0;
-    } else if (set == 1) {  // ghosts of the first tangential axis
-        const long long cnt = 2ll * (c.Nn + 1) * c.N2;
-        if (i >= cnt) return;
-        n = G + (int)(i % (c.Nn + 1));
-        long long r = i / (c.Nn + 1);
-        t2 = G + (int)(r % c.N2);
-        const int side = (int)(r / c.N2);
-        t1 = side ? G + c.N1 : G - 1;
-        const int s1 = side ? G + c.N1 - 1 : G;
-        val = flip(bc_src(c, G, n, s1, t2));
-    } else {  // ghosts of the second tangential axis (edges included)
-        const long long cnt = 2ll * (c.Nn + 1) * (c.N1 + 2);
-        if (i >= cnt) return;
-        n = G + (int)(i % (c.Nn + 1));
-        long long r = i / (c.Nn + 1);
-        t1 = G - 1 + (int)(r % (c.N1 + 2));
-        const int side = (int)(r / (c.N1 + 2));
-        t2 = side ? G + c.N2 : G - 1;
-        const int s2 = side ? G + c.N2 - 1 : G;
-        int s1 = t1;
-        bool odd = true;
-        if (t1 == G - 1) { s1 = G; odd = false; }
-        else if (t1 == G + c.N1) { s1 = G + c.N1 - 1; odd = false; }
-        const double s = bc_src(c, G, n, s1, s2);
-        val = odd ? flip(s) : s;
-    }
-    c.f[(long long)n * c.s_n + (long long)t1 * c.s_1 + (long long)t2 * c.s_2] = val;
+    const BcComp c = bc_comp(g, comp, u, v, w);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= bc_set_count(c, set)) return;
+    bc_cell(c, g.G, set, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -262,19 +178,7 @@ __global__ void k_divergence_fp64(Geom g, const double* __restrict__ u, const do
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z;
     if (x >= g.p.nx || y >= g.p.ny) return;
-    const long long i = x + y * g.p.sy + z * g.p.sz;
-    if (zero_p) p[i] = 0.0;
-    const int G = g.G;
-    if (x < G || x >= G + g.NX || y < G || y >= G + g.NY || z < G || z >= G + g.NZ) return;
-    const long long iu = x + y * g.u.sy + z * g.u.sz;
-    const long long iv = x + y * g.v.sy + z * g.v.sz;
-    const long long iw = x + y * g.w.sy + z * g.w.sz;
-    const double du = dsub(u[iu + 1], u[iu]);
-    const double dvv = dsub(v[iv + g.v.sy], v[iv]);
-    const double dw = dsub(w[iw + g.w.sz], w[iw]);
-    const double d = dmul(scale, dadd(dadd(du, dvv), dw));
-    dv[i] = d;
-    bb[i] = dmul(h2, d);
+    div_cell(g, u, v, w, p, dv, bb, scale, h2, zero_p != 0, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -307,37 +211,13 @@ __global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __rest
     p[i] = div6(dsub(sum, bb[i]));
 }
 
-// applyPressureBC, project.go:139-163: composed, every ghost of the first
-// layer holds the interior cell at the clamped coordinates.
+// applyPressureBC, project.go:139-163 (see pbc_cell).
 __global__ void k_pressure_bc(Geom g, double* __restrict__ p, Status* st, int gate) {
     if (gated(st, gate)) return;
-    const int G = g.G, NX = g.NX, NY = g.NY, NZ = g.NZ;
     const int set = blockIdx.y;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int x, y, z;
-    if (set == 0) {
-        if (i >= 2ll * NY * NZ) return;
-        y = G + (int)(i % NY);
-        long long r = i / NY;
-        z = G + (int)(r % NZ);
-        x = (r / NZ) ? G + NX : G - 1;
-    } else if (set == 1) {
-        if (i >= 2ll * (NX + 2) * NZ) return;
-        x = G - 1 + (int)(i % (NX + 2));
-        long long r = i / (NX + 2);
-        z = G + (int)(r % NZ);
-        y = (r / NZ) ? G + NY : G - 1;
-    } else {
-        if (i >= 2ll * (NX + 2) * (NY + 2)) return;
-        x = G - 1 + (int)(i % (NX + 2));
-        long long r = i / (NX + 2);
-        y = G - 1 + (int)(r % (NY + 2));
-        z = (r / (NY + 2)) ? G + NZ : G - 1;
-    }
-    const int cx = min(max(x, G), G + NX - 1);
-    const int cy = min(max(y, G), G + NY - 1);
-    const int cz = min(max(z, G), G + NZ - 1);
-    p[x + y * g.p.sy + z * g.p.sz] = p[cx + cy * g.p.sy + cz * g.p.sz];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pbc_set_count(g, set)) return;
+    pbc_cell(g, p, set, i);
 }
 
 // subtractGradient, project.go:172-205.
@@ -352,17 +232,7 @@ __global__ void k_gradient_fp64(Geom g, const double* __restrict__ p, double* __
     const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int x1 = G + g.NX + (c == 0), y1 = G + g.NY + (c == 1), z1 = G + g.NZ + (c == 2);
     if (x >= x1 || y >= y1 || z >= z1) return;
-    const long long ip = x + y * g.p.sy + z * g.p.sz;
-    if (c == 0) {
-        const long long i = x + y * g.u.sy + z * g.u.sz;
-        u[i] = dsub(u[i], dmul(scale, dsub(p[ip], p[ip - 1])));
-    } else if (c == 1) {
-        const long long i = x + y * g.v.sy + z * g.v.sz;
-        v[i] = dsub(v[i], dmul(scale, dsub(p[ip], p[ip - g.p.sy])));
-    } else {
-        const long long i = x + y * g.w.sy + z * g.w.sz;
-        w[i] = dsub(w[i], dmul(scale, dsub(p[ip], p[ip - g.p.sz])));
-    }
+    grad_face(g, p, u, v, w, scale, c, x, y, z);
 }
 
 __global__ void k_step_tick(Status* st) { st->step += 1; }
@@ -552,17 +422,15 @@ namespace {
 // Launchers
 // ---------------------------------------------------------------------------
 void launch_velocity_bc(const Geom& g, double* u, double* v, double* w, Status* st, int gate, cudaStream_t s) {
-    BcComp cu{u, 1, g.u.sy, g.u.sz, g.NX, g.NY, g.NZ};
-    BcComp cv{v, g.v.sy, 1, g.v.sz, g.NY, g.NX, g.NZ};
-    BcComp cw{w, g.w.sz, 1, g.w.sy, g.NZ, g.NX, g.NY};
     long long mx = 0;
-    for (const BcComp* c : {&cu, &cv, &cw}) {
-        mx = std::max(mx, 2ll * c->N1 * c->N2);
-        mx = std::max(mx, 2ll * (c->Nn + 1) * c->N2);
-        mx = std::max(mx, 2ll * (c->Nn + 1) * (c->N1 + 2));
+    const int N[3][3] = {{g.NX, g.NY, g.NZ}, {g.NY, g.NX, g.NZ}, {g.NZ, g.NX, g.NY}};  // Nn, N1, N2 per component
+    for (const auto& n : N) {
+        mx = std::max(mx, 2ll * n[1] * n[2]);
+        mx = std::max(mx, 2ll * (n[0] + 1) * n[2]);
+        mx = std::max(mx, 2ll * (n[0] + 1) * (n[1] + 2));
     }
     dim3 grid(cdiv(mx, 256), 9);
-    k_velocity_bc<<<grid, 256, 0, s>>>(cu, cv, cw, g.G, st, gate);
+    k_velocity_bc<<<grid, 256, 0, s>>>(g, u, v, w, st, gate);
 }
 
 void launch_sweep_fp64(const Geom& g, int axis, const Fields& f, double dt, double invH, double lam, Status* st,

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace af {
 
 // Field geometry on the device: padded extents and strides of grid.go:12-21.
@@ -79,6 +81,10 @@ void launch_max_abs3(const double* u, long long nu, const double* v, long long n
                      unsigned long long* out, cudaStream_t s);
 void launch_kinetic_energy(const Geom& g, const double* u, const double* v, const double* w, double* partials,
                            double* out, cudaStream_t s);
+
+// The reference's contained-fault text for a NaN backtrace recorded with
+// fault gate `gate` (step*8 + sweep phase) and fault key `key`.
+std::string fault_message_for(const Geom& g, unsigned gate, unsigned long long key);
 
 // Binary64 FMA issue rate of the current device (independent chains, timed
 // with events); false on a CUDA error.

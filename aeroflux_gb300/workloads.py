@@ -55,3 +55,67 @@ def taylor_green(cfg: Config, amp: float = 1.0, noise: float = 0.01, seed: int =
     if rc != L.AF_OK:
         raise ValueError("af_seed_taylor_green rejected the configuration")
     return u, v, w
+
+
+class Pcg32:
+    """PCG32 XSH-RR 64/32 (O'Neill 2014), pcg32_srandom_r seeding."""
+
+    M = (1 << 64) - 1
+
+    def __init__(self, seed: int, stream: int):
+        self.state, self.inc = 0, ((stream << 1) | 1) & self.M
+        self.next()
+        self.state = (self.state + seed) & self.M
+        self.next()
+
+    def next(self) -> int:
+        old = self.state
+        self.state = (old * 6364136223846793005 + self.inc) & self.M
+        xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xs >> rot) | (xs << ((32 - rot) & 31))) & 0xFFFFFFFF
+
+    def uniform(self) -> float:
+        a, b = self.next() >> 5, self.next() >> 6
+        return (a * 67108864.0 + b) * (1.0 / 9007199254740992.0)
+
+    def choice(self, seq):
+        return seq[int(self.uniform() * len(seq))]
+
+
+def _mixed_instance(rng: Pcg32, dims_choices, div_tol: float = 1e-10) -> Config:
+    nx, ny, nz = (rng.choice(dims_choices) for _ in range(3))
+    h = 1.0 / max(nx, ny, nz)
+    nu = 10.0 ** (-6.0 + 2.0 * rng.uniform())  # log-uniform in [1e-6, 1e-4]
+    dt = min(0.004, 0.5 * h * h / (6.0 * nu))
+    return Config(NX=nx, NY=ny, NZ=nz, H=h, DT=dt, Viscosity=nu, Density=1.0,
+                  Precision=L.AF_PRECISION_MIXED, DivTol=div_tol)
+
+
+BATCH_DIMS = (32, 48, 64, 96, 128)
+BATCH_STEPS = 300
+
+
+def batched_instances(n: int = 256, seed: int = 42) -> list[Config]:
+    """Uneven independent grids: each extent from {32,48,64,96,128}, H=1/max,
+    nu log-uniform in [1e-6,1e-4], DT=min(0.004, 0.5 H^2/(6 nu)), mixed form."""
+    rng = Pcg32(seed, 0xB47C4)
+    return [_mixed_instance(rng, BATCH_DIMS) for _ in range(n)]
+
+
+SERVE_DIMS = tuple(range(32, 193, 16))
+
+
+def served_requests(rate: float = 200.0, duration: float = 60.0, seed: int = 42):
+    """Poisson arrivals: (arrival time s, Config, steps), extents uniform over
+    multiples of 16 in [32,192], steps uniform in [50,500]."""
+    rng = Pcg32(seed, 0x5E7E)
+    t, out = 0.0, []
+    while True:
+        import math
+        t += -math.log(1.0 - rng.uniform()) / rate
+        if t >= duration:
+            return out
+        cfg = _mixed_instance(rng, SERVE_DIMS)
+        steps = 50 + int(rng.uniform() * 451)
+        out.append((t, cfg, steps))

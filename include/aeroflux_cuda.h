@@ -189,6 +189,50 @@ int af_last_step_profile(af_engine* e, af_step_profile* out);
  * in FMA instructions per second, for the FP64 roofline. */
 int af_device_fp64_rate(int device, double* fma_per_s);
 
+/* ---------------------------------------------------------------------------
+ * Batched and served form (no counterpart in the reference, which steps one
+ * grid per Engine): many MIXED-precision grids of uneven sizes in one batch.
+ * Every stage of a step is one persistent launch over device-side work lists
+ * covering all active slots, and the whole step is one CUDA graph with one
+ * refinement loop for the batch.  A slot computes the same bits alone (an
+ * af_create'd MIXED engine) and in any batch, under any tuning.  Slots can be
+ * assigned, released, activated and deactivated between steps without
+ * recapturing the graph, which is what continuous batching needs.
+ * ------------------------------------------------------------------------- */
+typedef struct af_batch af_batch;
+
+/* capacity slots on `device`; pool_bytes > 0 reserves one device pool of
+ * that size for all slot memory (the admission budget), 0 allocates per slot. */
+int af_batch_create(int64_t capacity, int64_t pool_bytes, int32_t device, af_batch** out, char* err, size_t errlen);
+/* Device bytes a slot with this config needs (after Normalize). */
+int af_batch_slot_bytes(const af_config* cfg, int64_t* bytes);
+/* Normalizes cfg (precision must be AF_PRECISION_MIXED) into a free slot;
+ * AF_ERR_NOMEM when the pool or the slots are exhausted.  Fields start zero. */
+int af_batch_assign(af_batch* b, const af_config* cfg, int64_t* slot);
+int af_batch_release(af_batch* b, int64_t slot);
+int af_batch_set_active(af_batch* b, int64_t slot, int active);
+int af_batch_get_config(const af_batch* b, int64_t slot, af_config* out);
+int af_batch_field_info(const af_batch* b, int64_t slot, int field, af_field_desc* out);
+int af_batch_field_upload(af_batch* b, int64_t slot, int field, const double* host, size_t count);
+int af_batch_field_download(af_batch* b, int64_t slot, int field, double* host, size_t count);
+/* applyVelocityBC of every active slot. */
+int af_batch_apply_velocity_bc(af_batch* b);
+/* nsteps Steps of every active slot.  Returns AF_OK when the batch ran,
+ * also if some slots faulted: query them with af_batch_slot_status. */
+int af_batch_step(af_batch* b, int64_t nsteps);
+/* faulted = 1 and the reference's message when the slot's last step faulted. */
+int af_batch_slot_status(af_batch* b, int64_t slot, int32_t* faulted, char* msg, size_t msglen);
+int af_batch_max_divergence(af_batch* b, int64_t slot, double* out);
+int af_batch_projection_stats(af_batch* b, int64_t slot, int64_t* passes, double* max_div);
+/* Autotuner: times candidate launch shapes of every stage on the current
+ * slots (run before uploading fields or between steps) and keeps the
+ * fastest; writes a JSON report.  Results are bit-identical under any shape. */
+int af_batch_tune(af_batch* b, int32_t reps, char* report, size_t len);
+int af_batch_profile(af_batch* b, int enable);
+int af_batch_last_step_profile(af_batch* b, af_step_profile* out);
+void af_batch_destroy(af_batch* b);
+const char* af_batch_last_error(const af_batch* b);
+
 /* Synthetic input (no counterpart in the reference API; its tests seed a
  * trigonometric field straight into arena views, engine_test.go:302-335).
  * Fills host arrays u, v, w -- the padded counts of U, V, W for the
