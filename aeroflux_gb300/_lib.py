@@ -45,6 +45,18 @@ class AfStepProfile(C.Structure):
                 ("rbgs_launches", C.c_int64), ("kernel_launches", C.c_int64)]
 
 
+class AfRequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("reserved", C.c_int32), ("cells", C.c_int64),
+                ("steps", C.c_int64), ("refinement_passes", C.c_int64), ("arrival_s", C.c_double),
+                ("admitted_s", C.c_double), ("completed_s", C.c_double), ("max_divergence", C.c_double)]
+
+
+class AfServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int64), ("resident", C.c_int64), ("retained", C.c_int64),
+                ("budget_bytes", C.c_int64), ("used_bytes", C.c_int64), ("executed_cell_steps", C.c_int64),
+                ("now_s", C.c_double)]
+
+
 class AfFieldDesc(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("off", "nx", "ny", "nz", "sy", "sz", "count")]
 
@@ -79,6 +91,7 @@ SIGNATURES = {
     "af_profile": (C.c_int, [_E, C.c_int]),
     "af_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
     "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "af_selftest_div6": (C.c_int, [C.c_int, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "af_batch_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.POINTER(_E), *_ERR]),
     "af_batch_slot_bytes": (C.c_int, [C.POINTER(AfConfig), C.POINTER(C.c_int64)]),
     "af_batch_assign": (C.c_int, [_E, C.POINTER(AfConfig), C.POINTER(C.c_int64)]),
@@ -96,12 +109,27 @@ SIGNATURES = {
     "af_batch_tune": (C.c_int, [_E, C.c_int32, *_ERR]),
     "af_batch_profile": (C.c_int, [_E, C.c_int]),
     "af_batch_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
+    "af_batch_seed": (C.c_int, [_E, C.c_int64, C.c_double, C.c_double, C.c_uint64, C.c_uint64]),
     "af_batch_destroy": (None, [_E]),
+    "af_server_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_E),
+                                   *_ERR]),
+    "af_server_now": (C.c_int, [_E, C.POINTER(C.c_double)]),
+    "af_server_submit": (C.c_int, [_E, C.POINTER(AfConfig), C.c_int64, C.c_uint64, C.c_double,
+                                   C.POINTER(C.c_int64)]),
+    "af_server_round": (C.c_int, [_E, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "af_server_results": (C.c_int, [_E, C.POINTER(AfRequestResult), C.c_int64, C.POINTER(C.c_int64)]),
+    "af_server_download": (C.c_int, [_E, C.c_int64, C.c_int, C.c_void_p, C.c_size_t]),
+    "af_server_release": (C.c_int, [_E, C.c_int64]),
+    "af_server_get_stats": (C.c_int, [_E, C.POINTER(AfServerStats)]),
+    "af_server_tune": (C.c_int, [_E, C.c_int32, *_ERR]),
+    "af_server_destroy": (None, [_E]),
+    "af_server_last_error": (C.c_char_p, [_E]),
     "af_batch_last_error": (C.c_char_p, [_E]),
     "af_seed_taylor_green": (C.c_int, [C.POINTER(AfConfig), C.c_double, C.c_double, C.c_uint64, C.c_uint64,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "af_kinetic_energy_noalloc": (C.c_int, [C.POINTER(AfConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.POINTER(C.c_double), *_ERR]),
+    "af_seed_device": (C.c_int, [_E, C.c_double, C.c_double, C.c_uint64, C.c_uint64]),
     "af_close": (C.c_int, [_E]),
     "af_destroy": (None, [_E]),
     "af_last_error": (C.c_char_p, [_E]),

@@ -68,6 +68,10 @@ class Batch:
         self._check(L.lib().af_batch_field_download(self._h, slot, FIELD_IDS[name], out.ctypes.data, out.size))
         return out
 
+    def seed(self, slot: int, amp: float = 1.0, noise: float = 0.01, seed: int = 42, stream: int = 0) -> None:
+        """Device-side Taylor-Green + PCG32 initial field (then apply the BC)."""
+        self._check(L.lib().af_batch_seed(self._h, slot, amp, noise, seed, stream))
+
     def apply_velocity_bc(self) -> None:
         self._check(L.lib().af_batch_apply_velocity_bc(self._h))
 

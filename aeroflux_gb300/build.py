@@ -29,6 +29,7 @@ UNITS = {
     "af_fp64.cu": ["--fmad=false"],
     "af_batch.cu": [],
     "af_workload.cu": [],
+    "af_serve.cu": [],
 }
 
 

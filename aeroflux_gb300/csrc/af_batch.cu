@@ -42,12 +42,29 @@ constexpr int kMaxLev = 16;
 constexpr int kCoarseThreads = 512;
 constexpr int kCoarseMax = 4096;
 
+// Unsigned 32-bit division by an invariant divisor with one multiply-high
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994): l = ceil(log2 d), m = ceil(2^(32+l)/d) - 2^32,
+// n/d = (umulhi(n, m) + n) >> l for every n < 2^32.
+struct FastDiv {
+    unsigned d = 1, m = 0, l = 0;
+    FastDiv() = default;
+    __host__ explicit FastDiv(unsigned div) : d(div) {
+        while ((1ull << l) < d) ++l;
+        m = (unsigned)((((1ull << (32 + l)) + d - 1) / d) - (1ull << 32));
+    }
+    __device__ __forceinline__ unsigned div(unsigned n) const {
+        return (unsigned)(((unsigned long long)__umulhi(n, m) + n) >> l);
+    }
+};
+
 struct Lvl {
     int nx, ny, nz;
     float wx, wy, wz;   // (h0 / h_axis)^2
     int cx, cy, cz;     // 1 when the axis coarsens into the next level
     float* e;
     float* r;
+    FastDiv fnx, fny, fhx;  // nx, ny, (nx+1)/2
 };
 
 struct Ctl {
@@ -73,6 +90,9 @@ struct InstDev {
     int coarse_sweeps;  // > 0: one-block coarse solve; 0: smoothing at the coarsest level
     int parity;         // 1 when U/V/W live in the Tmp slots
     int active;
+    FastDiv fpx, fpy;        // padded P extents
+    FastDiv ffx, ffy, ffz;   // NX+1, NY+1, NZ+1 (the face box)
+    FastDiv fnx, fny;        // NX, NY
     Lvl lev[kMaxLev];
 };
 
@@ -179,10 +199,9 @@ __global__ void kb_div(const InstDev* inst, Status* st, Tab tab, int parity, int
     const long long n = (long long)g.p.nx * g.p.ny * g.p.nz;
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int x = (int)(el % g.p.nx);
-    const long long r = el / g.p.nx;
+    const unsigned e = (unsigned)el, r = I.fpx.div(e), z = I.fpy.div(r);
     div_cell(g, cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.slot[0], I.slot[4], I.b, I.div_scale,
-             I.h2, true, x, (int)(r % g.p.ny), (int)(r / g.p.ny));
+             I.h2, true, (int)(e - r * g.p.nx), (int)(r - z * g.p.ny), (int)z);
     END_ELEMS
     END_TILES
 }
@@ -202,13 +221,13 @@ __global__ void kb_pbc(const InstDev* inst, Status* st, Tab tab, int gate) {
     END_TILES
 }
 
-__device__ __forceinline__ bool face_of(const Geom& g, long long el, int* c, int* x, int* y, int* z) {
-    *x = g.G + (int)(el % (g.NX + 1));
-    long long r = el / (g.NX + 1);
-    *y = g.G + (int)(r % (g.NY + 1));
-    r /= (g.NY + 1);
-    *c = (int)(r / (g.NZ + 1));
-    *z = g.G + (int)(r % (g.NZ + 1));
+__device__ __forceinline__ bool face_of(const InstDev& I, long long el, int* c, int* x, int* y, int* z) {
+    const Geom& g = I.g;
+    const unsigned e = (unsigned)el, r = I.ffx.div(e), r2 = I.ffy.div(r), cc = I.ffz.div(r2);
+    *x = g.G + (int)(e - r * (unsigned)(g.NX + 1));
+    *y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1));
+    *z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
+    *c = (int)cc;
     return *x < g.G + g.NX + (*c == 0) && *y < g.G + g.NY + (*c == 1) && *z < g.G + g.NZ + (*c == 2);
 }
 
@@ -220,7 +239,7 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
     FOR_ELEMS(tab)
     if (el >= n) break;
     int c, x, y, z;
-    if (face_of(I.g, el, &c, &x, &y, &z))
+    if (face_of(I, el, &c, &x, &y, &z))
         grad_face(I.g, I.slot[0], cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.grad_scale, c, x, y, z);
     END_ELEMS
     END_TILES
@@ -241,7 +260,7 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
     FOR_ELEMS(tab)
     if (el >= n) break;
     int c, x, y, z;
-    if (face_of(I.g, el, &c, &x, &y, &z) && !mx_sweep_face<AX>(I.g, u, v, w, tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
+    if (face_of(I, el, &c, &x, &y, &z) && !mx_sweep_face<AX>(I.g, u, v, w, tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
         atomicMin(&st[s].fault_gate, st[s].step * 8u + (unsigned)phase);
         atomicMin(&st[s].fault_key, fault_key(c, x, y, z));
     }
@@ -267,45 +286,65 @@ __global__ void kb_init(const InstDev* inst, Ctl* ctl, int n) {
 // r = b - L(p) in binary64 over the interior, r (binary32) for the inner
 // solve, inner solution zeroed, max|r| reduced per slot.  In the loop a
 // converged slot is skipped.
-__global__ void kb_residual(const InstDev* inst, Status* st, Ctl* ctl, Tab tab, int gate, int in_loop) {
-    FOR_TILES(tab)
-    const InstDev& I = inst[s];
-    if (gated(&st[s], gate) || (in_loop && ctl[s].stopped)) continue;
-    const Geom& g = I.g;
-    const double* p = I.slot[0];
-    const long long n = (long long)g.NX * g.NY * g.NZ;
-    unsigned long long m = 0;
-    FOR_ELEMS(tab)
-    if (el < n) {
-        const int xi = (int)(el % g.NX);
-        const long long r2 = el / g.NX;
-        const int yi = (int)(r2 % g.NY), zi = (int)(r2 / g.NY);
-        const long long sy = g.p.sy, sz = g.p.sz;
-        const long long i = (g.G + xi) + (g.G + yi) * sy + (g.G + zi) * sz;
-        const double pc = p[i];
-        const double xm = xi > 0 ? p[i - 1] : pc;
-        const double xp = xi < g.NX - 1 ? p[i + 1] : pc;
-        const double ym = yi > 0 ? p[i - sy] : pc;
-        const double yp = yi < g.NY - 1 ? p[i + sy] : pc;
-        const double zm = zi > 0 ? p[i - sz] : pc;
-        const double zp = zi < g.NZ - 1 ? p[i + sz] : pc;
-        const double res = I.b[i] - fma(-6.0, pc, ((xm + xp) + (ym + yp)) + (zm + zp));
-        I.lev[0].r[el] = f64_to_f32(res);
-        I.lev[0].e[el] = 0.0f;
-        // |res| and NaN tested on the bit pattern (integer pipe); NaN reads as
-        // +Inf so the loop stops.
-        const unsigned long long a = (unsigned long long)__double_as_longlong(res) & ~kSign;
-        const unsigned long long v = a > 0x7FF0000000000000ull ? 0x7FF0000000000000ull : a;
-        m = v > m ? v : m;
-    }
-    END_ELEMS
+__device__ __forceinline__ void warp_max_commit(unsigned long long m, unsigned long long* out) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
         m = t > m ? t : m;
     }
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctl[s].maxr_bits, m);
-    END_TILES
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// r = b - L(p) in binary64 over the interior, r (binary32) for the inner
+// solve, inner solution zeroed, max|r| reduced per slot.  A block keeps its
+// running maximum over consecutive tiles of one slot and commits it (one
+// atomic per warp) when the slot changes or the block finishes, so the
+// atomics are per block, not per warp-sized tile.  In the loop a converged
+// slot is skipped.
+__global__ void kb_residual(const InstDev* inst, Status* st, Ctl* ctl, Tab tab, int gate, int in_loop) {
+    int held = -1;
+    unsigned long long m = 0;
+    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
+        const int s = find_slot(tab.prefix, tab.n, item);
+        const long long first = (long long)(item - tab.prefix[s]) * blockDim.x * tab.ept;
+        const InstDev& I = inst[s];
+        if (gated(&st[s], gate) || (in_loop && ctl[s].stopped)) continue;
+        if (s != held) {
+            if (held >= 0) warp_max_commit(m, &ctl[held].maxr_bits);
+            held = s;
+            m = 0;
+        }
+        const Geom& g = I.g;
+        const double* __restrict__ p = I.slot[0];
+        const double* __restrict__ bb = I.b;
+        float* __restrict__ r0 = I.lev[0].r;
+        float* __restrict__ e0 = I.lev[0].e;
+        const long long n = (long long)g.NX * g.NY * g.NZ;
+        for (int k = 0; k < tab.ept; ++k) {
+            const long long el = first + (long long)k * blockDim.x + threadIdx.x;
+            if (el >= n) continue;
+            const unsigned e = (unsigned)el, r2 = I.fnx.div(e), zz = I.fny.div(r2);
+            const int xi = (int)(e - r2 * (unsigned)g.NX), yi = (int)(r2 - zz * (unsigned)g.NY), zi = (int)zz;
+            const long long sy = g.p.sy, sz = g.p.sz;
+            const long long i = (g.G + xi) + (g.G + yi) * sy + (g.G + zi) * sz;
+            const double pc = p[i];
+            const double xm = xi > 0 ? p[i - 1] : pc;
+            const double xp = xi < g.NX - 1 ? p[i + 1] : pc;
+            const double ym = yi > 0 ? p[i - sy] : pc;
+            const double yp = yi < g.NY - 1 ? p[i + sy] : pc;
+            const double zm = zi > 0 ? p[i - sz] : pc;
+            const double zp = zi < g.NZ - 1 ? p[i + sz] : pc;
+            const double res = bb[i] - fma(-6.0, pc, ((xm + xp) + (ym + yp)) + (zm + zp));
+            r0[el] = f64_to_f32(res);
+            e0[el] = 0.0f;
+            // |res| and NaN on the bit pattern (integer pipe); NaN reads as
+            // +Inf so the loop stops.
+            const unsigned long long a = (unsigned long long)__double_as_longlong(res) & ~kSign;
+            const unsigned long long v = a > 0x7FF0000000000000ull ? 0x7FF0000000000000ull : a;
+            m = v > m ? v : m;
+        }
+    }
+    if (held >= 0) warp_max_commit(m, &ctl[held].maxr_bits);
 }
 
 __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
@@ -316,9 +355,9 @@ __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
     const long long n = (long long)g.NX * g.NY * g.NZ;
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int xi = (int)(el % g.NX);
-    const long long r2 = el / g.NX;
-    const long long i = (g.G + xi) + (g.G + (int)(r2 % g.NY)) * g.p.sy + (g.G + (int)(r2 / g.NY)) * g.p.sz;
+    const unsigned e = (unsigned)el, r2 = I.fnx.div(e), zz = I.fny.div(r2);
+    const long long i = (g.G + (int)(e - r2 * (unsigned)g.NX)) + (g.G + (int)(r2 - zz * (unsigned)g.NY)) * g.p.sy +
+                        (g.G + (int)zz) * g.p.sz;
     I.slot[0][i] += f32_to_f64(I.lev[0].e[el]);
     END_ELEMS
     END_TILES
@@ -362,9 +401,8 @@ __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, i
     const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int k = (int)(el % hx);
-    const long long r = el / hx;
-    const int y = (int)(r % L.ny), z = (int)(r / L.ny);
+    const unsigned e = (unsigned)el, r = L.fhx.div(e), zz = L.fny.div(r);
+    const int k = (int)(e - r * (unsigned)hx), y = (int)(r - zz * (unsigned)L.ny), z = (int)zz;
     const int x = (((y + z) & 1) != color ? 1 : 0) + 2 * k;
     if (x < L.nx) {
         const long long i = lidx(x, y, z, L.nx, L.ny);
@@ -399,9 +437,8 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l)
     const float inv = 1.0f / (float)(ex * ey * ez);
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int X = (int)(el % C.nx);
-    const long long r = el / C.nx;
-    const int Y = (int)(r % C.ny), Z = (int)(r / C.ny);
+    const unsigned e = (unsigned)el, r = C.fnx.div(e), zz = C.fny.div(r);
+    const int X = (int)(e - r * (unsigned)C.nx), Y = (int)(r - zz * (unsigned)C.ny), Z = (int)zz;
     float sum = 0.0f;
     for (int dz = 0; dz < ez; ++dz)
         for (int dy = 0; dy < ey; ++dy)
@@ -423,9 +460,8 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l) 
     const long long n = lvl_cells(F);
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int x = (int)(el % F.nx);
-    const long long r = el / F.nx;
-    const int y = (int)(r % F.ny), z = (int)(r / F.ny);
+    const unsigned e = (unsigned)el, r = F.fnx.div(e), zz = F.fny.div(r);
+    const int x = (int)(e - r * (unsigned)F.nx), y = (int)(r - zz * (unsigned)F.ny), z = (int)zz;
     int X0 = x, X1 = x, Y0 = y, Y1 = y, Z0 = z, Z1 = z;
     float ax = 1.0f, ay = 1.0f, az = 1.0f;
     if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
@@ -499,6 +535,65 @@ __global__ void __launch_bounds__(kCoarseThreads) kb_coarse(const InstDev* inst,
         const float mean_e = block_sum(part, red) / (float)n;
         for (int i = threadIdx.x; i < n; i += kCoarseThreads) L.e[i] = se[i] - mean_e;
         __syncthreads();
+    }
+}
+
+// --- device-side synthetic initial field ---------------------------------
+// The Taylor-Green vortex plus PCG32 noise of af_seed_taylor_green, generated
+// in parallel: draw k (two PCG outputs) of the sequential U, V, W; z, y, x
+// order comes from jumping the generator ahead 2k steps (F. Brown, "Random
+// number generation with arbitrary strides", 1994, the pcg32_advance
+// method).  The trigonometric factors use binary32 sinpi/cospi, so the field
+// is bit-reproducible on the device but not identical to the host
+// generator's libm values.
+__device__ __forceinline__ unsigned long long pcg_advance(unsigned long long state, unsigned long long inc,
+                                                          unsigned long long delta) {
+    unsigned long long cur_mult = 6364136223846793005ull, cur_plus = inc, acc_mult = 1ull, acc_plus = 0ull;
+    while (delta > 0) {
+        if (delta & 1ull) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1ull) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    return acc_mult * state + acc_plus;
+}
+
+__device__ __forceinline__ unsigned pcg_output(unsigned long long old) {
+    const unsigned xorshifted = (unsigned)(((old >> 18u) ^ old) >> 27u);
+    const unsigned rot = (unsigned)(old >> 59u);
+    return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+}
+
+__global__ void k_seed_tg(Geom g, double* u, double* v, double* w, float H, unsigned long long state0,
+                          unsigned long long inc, double amp, double noise) {
+    const long long cu = (long long)(g.NX + 1) * g.NY * g.NZ, cv = (long long)g.NX * (g.NY + 1) * g.NZ,
+                    cw = (long long)g.NX * g.NY * (g.NZ + 1);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < cu + cv + cw;
+         k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long st = pcg_advance(state0, inc, 2ull * (unsigned long long)k);
+        const unsigned a = pcg_output(st) >> 5;
+        const unsigned b = pcg_output(st * 6364136223846793005ull + inc) >> 6;
+        const double uni = ((double)a * 67108864.0 + (double)b) * (1.0 / 9007199254740992.0);
+        int comp, ex, ey;
+        long long r;
+        if (k < cu) { comp = 0; r = k; ex = g.NX + 1; ey = g.NY; }
+        else if (k < cu + cv) { comp = 1; r = k - cu; ex = g.NX; ey = g.NY + 1; }
+        else { comp = 2; r = k - cu - cv; ex = g.NX; ey = g.NY; }
+        const int x = (int)(r % ex), y = (int)((r / ex) % ey), z = (int)(r / ((long long)ex * ey));
+        // Staggered face positions: u at (i, j+1/2, k+1/2) H, v at (i+1/2, j, k+1/2) H.
+        const float X = ((float)x + (comp == 0 ? 0.0f : 0.5f)) * H;
+        const float Y = ((float)y + (comp == 1 ? 0.0f : 0.5f)) * H;
+        const float Z = ((float)z + 0.5f) * H;
+        float tg = 0.0f;
+        if (comp == 0) tg = sinpif(2.0f * X) * cospif(2.0f * Y) * cospif(2.0f * Z);
+        else if (comp == 1) tg = -cospif(2.0f * X) * sinpif(2.0f * Y) * cospif(2.0f * Z);
+        const double val = amp * (double)tg + noise * (2.0 * uni - 1.0);
+        double* f = comp == 0 ? u : (comp == 1 ? v : w);
+        const Dims& d = comp == 0 ? g.u : (comp == 1 ? g.v : g.w);
+        f[(x + g.G) + (long long)(y + g.G) * d.sy + (long long)(z + g.G) * d.sz] = val;
     }
 }
 
@@ -587,6 +682,7 @@ struct Batch {
     Shape shape[S_COUNT];
     int grid_sz[S_COUNT] = {};       // blocks per stage, fixed when the graph is captured
     int graph_levels = 0;            // levels the captured graph covers
+    unsigned graph_big = 0;          // levels whose large-coarsest smoothing the graph carries
     cudaGraphExec_t graph = nullptr;
     bool tables_dirty = true;
     bool profiling = false;
@@ -604,6 +700,15 @@ int max_levels(const Batch* b) {
     int m = 1;
     for (const auto& s : b->slots)
         if (s.used) m = std::max(m, s.d.nlev);
+    return m;
+}
+
+// Levels at which some slot's coarsest grid is too large for the one-block
+// solver (smoothed in place instead).
+unsigned big_coarse_levels(const Batch* b) {
+    unsigned m = 0;
+    for (const auto& s : b->slots)
+        if (s.used && s.d.coarse_sweeps == 0) m |= 1u << (s.d.nlev - 1);
     return m;
 }
 
@@ -710,7 +815,8 @@ void enq_vcycle(Batch* b, cudaStream_t s) {
         LAUNCH(b, S_RESTRICT + l, kb_restrict, b->d_inst, b->d_ctl, tab(b, S_RESTRICT + l), l);
     }
     LAUNCH(b, S_COARSE, kb_coarse, b->d_inst, b->d_ctl, tab(b, S_COARSE));
-    for (int l = 0; l < L; ++l) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, s);
+    for (int l = 0; l < L; ++l)
+        if (b->graph_big & (1u << l)) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, s);
     for (int l = L - 2; l >= 0; --l) {
         LAUNCH(b, S_PROLONG + l, kb_prolong, b->d_inst, b->d_ctl, tab(b, S_PROLONG + l), l);
         enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
@@ -831,12 +937,14 @@ cudaError_t prepare(Batch* b) {
     cudaError_t rc;
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     const int L = max_levels(b);
-    if (b->graph && L > b->graph_levels) {
+    const unsigned big = big_coarse_levels(b);
+    if (b->graph && (L > b->graph_levels || (big & ~b->graph_big))) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
     if (!b->graph) {
         b->graph_levels = std::max(L, b->graph_levels);
+        b->graph_big |= big;
         b->launches = 0;
         size_grids(b);
         if ((rc = capture(b, [&] { enq_step(b, b->stream); }, &b->graph)) != cudaSuccess) {
@@ -924,7 +1032,8 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
     float wx = 1.0f, wy = 1.0f, wz = 1.0f;
     while (true) {
         Lvl& L = lev[n++];
-        L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr};
+        L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr,
+                FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2))};
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
         if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;
@@ -1014,6 +1123,19 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.g.u = dims_of(S.desc[1]);
     I.g.v = dims_of(S.desc[2]);
     I.g.w = dims_of(S.desc[3]);
+    if (face_box(I.g) >= (1ll << 32) || S.desc[1].count >= (1ll << 31) || S.desc[2].count >= (1ll << 31) ||
+        S.desc[3].count >= (1ll << 31)) {
+        *err = "aeroflux: grid too large for one batch slot (2^31 elements per field)";
+        S = SlotHost();
+        return -1;
+    }
+    I.fpx = FastDiv((unsigned)I.g.p.nx);
+    I.fpy = FastDiv((unsigned)I.g.p.ny);
+    I.ffx = FastDiv((unsigned)(I.g.NX + 1));
+    I.ffy = FastDiv((unsigned)(I.g.NY + 1));
+    I.ffz = FastDiv((unsigned)(I.g.NZ + 1));
+    I.fnx = FastDiv((unsigned)I.g.NX);
+    I.fny = FastDiv((unsigned)I.g.NY);
     I.nlev = plan_levels(I.g.NX, I.g.NY, I.g.NZ, I.lev, &I.coarse_sweeps);
     const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
     const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
@@ -1127,6 +1249,7 @@ cudaError_t batch_project(Batch* b, std::string* err) {
         b->graph = nullptr;
     }
     b->graph_levels = std::max(b->graph_levels, max_levels(b));
+    b->graph_big |= big_coarse_levels(b);
     size_grids(b);
     cudaGraphExec_t g = nullptr;
     const bool prof = b->profiling;
@@ -1182,6 +1305,31 @@ cudaError_t batch_sweep(Batch* b, int axis, double dt) {
         if (b->slots[i].used && b->slots[i].active && st[i].fault_gate == kNoFault) b->slots[i].d.parity ^= 1;
     b->tables_dirty = true;
     return cudaSuccess;
+}
+
+cudaError_t batch_seed(Batch* b, int s, double amp, double noise, uint64_t seed, uint64_t stream) {
+    SlotHost& S = b->slots[s];
+    if (!S.used) return cudaErrorInvalidValue;
+    // The fields start from zero (as after New), then the write ranges are set.
+    for (int f = 1; f <= 3; ++f) cudaMemsetAsync(S.d.slot[f], 0, (size_t)S.desc[f].count * 8, b->stream);
+    for (int f = 5; f <= 7; ++f) cudaMemsetAsync(S.d.slot[f], 0, (size_t)S.desc[f].count * 8, b->stream);
+    S.d.parity = 0;
+    b->tables_dirty = true;
+    return seed_tg_fields(S.d.g, S.d.slot[1], S.d.slot[2], S.d.slot[3], S.cfg.h, amp, noise, seed, stream, b->stream);
+}
+
+cudaError_t seed_tg_fields(const Geom& g, double* u, double* v, double* w, double h, double amp, double noise,
+                           uint64_t seed, uint64_t stream, cudaStream_t s) {
+    // pcg32_srandom_r(seed, stream): state 0, one step, add the seed, one step.
+    const unsigned long long inc = (stream << 1u) | 1u;
+    unsigned long long st = inc;
+    st += seed;
+    st = st * 6364136223846793005ull + inc;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_seed_tg<<<sms * 4, 256, 0, s>>>(g, u, v, w, (float)h, st, inc, amp, noise);
+    return cudaGetLastError();
 }
 
 int batch_collect_faults(Batch* b, std::string* msg, int* first_slot) {

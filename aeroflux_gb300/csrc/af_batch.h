@@ -47,6 +47,10 @@ cudaError_t batch_velocity_bc(Batch* b);
 // One sweep (dispatch + commit) of every active slot.
 cudaError_t batch_sweep(Batch* b, int axis, double dt);
 
+// Writes the seeded Taylor-Green + PCG32 noise initial field of a slot on
+// the device (U, V, W zeroed first); apply the velocity BC afterwards.
+cudaError_t batch_seed(Batch* b, int slot, double amp, double noise, uint64_t seed, uint64_t stream);
+
 // Reads every slot's status after the enqueued work: returns the number of
 // slots that faulted in it; `msg` gets the first faulting slot's message.
 int batch_collect_faults(Batch* b, std::string* msg, int* first_slot);

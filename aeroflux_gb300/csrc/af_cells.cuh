@@ -40,6 +40,32 @@ __device__ __forceinline__ double div6(double x) {
     return x / 6.0;
 }
 
+// Correctly rounded x/6 on the integer pipe.  For normal x with significand
+// M (53-bit integer) and biased exponent E, x/6 = 2^(E-1076-t) * (M*2^t/3)
+// with t = 1 when M >= 3*2^51, else t = 2, which puts N/3 (N = M*2^t) in
+// [2^52, 2^53).  Q = floor(N/3) by a multiply-high with the 2^65/3 magic
+// constant (exact for every 64-bit N); the remainder N - 3Q is 0, 1 or 2, so
+// the fraction is 0, 1/3 or 2/3: round up exactly when it is 2 (no ties).
+// Zero, subnormal, Inf, NaN and results that would be subnormal (E < 5) take
+// the IEEE division.  No binary64 arithmetic instruction is issued.
+__device__ __forceinline__ double div6_int(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned E = (unsigned)(b >> 52) & 0x7FFu;
+    if (E < 5u || E == 0x7FFu) return x / 6.0;
+    const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    const unsigned t = M >= 0x18000000000000ull ? 1u : 2u;  // 3*2^51
+    const unsigned long long N = M << t;
+    unsigned long long Q = __umul64hi(N, 0xAAAAAAAAAAAAAAABull) >> 1;
+    const unsigned long long rem = N - 3ull * Q;
+    unsigned long long e = (unsigned long long)(E - 1u - t);
+    Q += rem == 2ull ? 1ull : 0ull;
+    if (Q == 0x20000000000000ull) {  // rounded up to 2^53
+        Q >>= 1;
+        e += 1;
+    }
+    return __longlong_as_double((long long)((b & kSign) | (e << 52) | (Q & 0xFFFFFFFFFFFFFull)));
+}
+
 __device__ __forceinline__ bool gated(const Status* st, int gate) {
     return st->fault_gate < st->step * 8u + (unsigned)gate;
 }

@@ -518,6 +518,10 @@ int af_create(const af_config* cin, af_engine** out, char* err, size_t errlen) {
             e->err = merr;
             return fail(AF_ERR_NOMEM);
         }
+        // Pick launch shapes while every field is still zero (results do not
+        // depend on them); AEROFLUX_NO_TUNE=1 keeps the defaults.
+        const char* nt = getenv("AEROFLUX_NO_TUNE");
+        if (!(nt && nt[0] == '1')) af::batch_tune(e->batch, 2);
     }
     if ((rc = reset_status(e)) != AF_OK) return fail(rc);
     if ((cr = cudaStreamSynchronize(e->stream)) != cudaSuccess)
@@ -810,10 +814,31 @@ int af_last_step_profile(af_engine* e, af_step_profile* out) {
     return AF_OK;
 }
 
+int af_selftest_div6(int device, int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (!mismatches || n < 0 || device < 0) return AF_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return AF_ERR_CUDA;
+    unsigned long long bad = 0;
+    if (!af::selftest_div6((unsigned long long)n, seed, &bad)) return AF_ERR_CUDA;
+    *mismatches = (int64_t)bad;
+    return AF_OK;
+}
+
 int af_device_fp64_rate(int device, double* fma_per_s) {
     if (!fma_per_s || device < 0) return AF_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return AF_ERR_CUDA;
     return af::measure_fp64_rate(fma_per_s) ? AF_OK : AF_ERR_CUDA;
+}
+
+int af_seed_device(af_engine* e, double amp, double noise, uint64_t seed, uint64_t stream) {
+    if (int rc = check_open(e)) return rc;
+    Fields f = e->fields();
+    double* zero[6] = {f.u, f.v, f.w, f.t0, f.t1, f.t2};
+    const int ids[6] = {AF_FIELD_U, AF_FIELD_V, AF_FIELD_W, AF_FIELD_TMP0, AF_FIELD_TMP1, AF_FIELD_TMP2};
+    for (int k = 0; k < 6; ++k)
+        AF_CUDA(e, cudaMemsetAsync(zero[k], 0, (size_t)e->current(ids[k], nullptr).count * 8, e->stream));
+    AF_CUDA(e, af::seed_tg_fields(e->geom, f.u, f.v, f.w, e->cfg.h, amp, noise, seed, stream, e->stream));
+    AF_CUDA(e, cudaStreamSynchronize(e->stream));
+    return AF_OK;
 }
 
 int af_close(af_engine* e) {
@@ -1038,6 +1063,14 @@ int af_batch_last_step_profile(af_batch* h, af_step_profile* out) {
     if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, "aeroflux: profiling is off or no step has run");
     *out = p;
     return AF_OK;
+}
+
+int af_batch_seed(af_batch* h, int64_t slot, double amp, double noise, uint64_t seed, uint64_t stream) {
+    if (!batch_slot_ok(h, slot)) return AF_ERR_ARG;
+    cudaSetDevice(h->device);
+    cudaError_t rc = af::batch_seed(h->b, (int)slot, amp, noise, seed, stream);
+    if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, sfmt("aeroflux: cuda: %s", cudaGetErrorString(rc)));
+    return batch_wait(h);
 }
 
 void af_batch_destroy(af_batch* h) {

@@ -208,7 +208,7 @@ __global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __rest
     const double zm = z > G ? p[i - sz] : pc;
     const double zp = z < G + g.NZ - 1 ? p[i + sz] : pc;
     const double sum = dadd(dadd(dadd(dadd(dadd(xm, xp), ym), yp), zm), zp);
-    p[i] = div6(dsub(sum, bb[i]));
+    p[i] = div6_int(dsub(sum, bb[i]));
 }
 
 // applyPressureBC, project.go:139-163 (see pbc_cell).
@@ -370,6 +370,29 @@ __global__ void __launch_bounds__(kKeThreads) k_ke_final(const double* partials,
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// Self-test of the exact /6 forms against IEEE division over PCG32-random
+// doubles: uniform significands, exponents spread over the whole range
+// (including subnormals, zero, Inf and NaN patterns).  Counts mismatching
+// bit patterns (NaNs compare by NaN-ness).
+__global__ void k_selftest_div6(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        // splitmix64 of (seed, i): every input independent of the launch shape
+        unsigned long long z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const double x = __longlong_as_double((long long)z);
+        const double ref = x / 6.0;
+        const double a = div6_int(x), c = div6(x);
+        const bool ok_a = __double_as_longlong(a) == __double_as_longlong(ref) || (isnan(a) && isnan(ref));
+        const bool ok_c = __double_as_longlong(c) == __double_as_longlong(ref) || (isnan(c) && isnan(ref));
+        local += (ok_a ? 0 : 1) + (ok_c ? 0 : 1);
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 // Eight independent DFMA chains per thread: issue-rate bound, not latency bound.
 constexpr int kRateIters = 2048, kRateChains = 8;
 __global__ void k_fp64_rate(double* out, double seed) {
@@ -388,6 +411,16 @@ __global__ void k_fp64_rate(double* out, double seed) {
 }
 
 }  // namespace
+
+bool selftest_div6(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
+    unsigned long long* bad = nullptr;
+    if (cudaMalloc(&bad, sizeof *bad) != cudaSuccess) return false;
+    cudaMemset(bad, 0, sizeof *bad);
+    k_selftest_div6<<<152 * 8, 256>>>(n, seed, bad);
+    const bool ok = cudaMemcpy(mismatches, bad, sizeof *bad, cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(bad);
+    return ok && cudaGetLastError() == cudaSuccess;
+}
 
 bool measure_fp64_rate(double* fma_per_s) {
     int dev = 0, sms = 0;

@@ -86,6 +86,15 @@ void launch_kinetic_energy(const Geom& g, const double* u, const double* v, cons
 // fault gate `gate` (step*8 + sweep phase) and fault key `key`.
 std::string fault_message_for(const Geom& g, unsigned gate, unsigned long long key);
 
+// Writes the seeded Taylor-Green + PCG32 noise initial field into the write
+// ranges of u, v, w (device, af_batch.cu).
+cudaError_t seed_tg_fields(const Geom& g, double* u, double* v, double* w, double h, double amp, double noise,
+                           uint64_t seed, uint64_t stream, cudaStream_t s);
+
+// Compares both exact /6 forms with IEEE division on n random bit patterns
+// (af_fp64.cu); false on a CUDA error.
+bool selftest_div6(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
+
 // Binary64 FMA issue rate of the current device (independent chains, timed
 // with events); false on a CUDA error.
 bool measure_fp64_rate(double* fma_per_s);

@@ -1,0 +1,169 @@
+"""Serving over the C ABI (af_server_*): continuous batching of simulation
+requests of different sizes, admitted by device-memory budget, state resident
+on the device, p50/p99 completion latency beside throughput.
+
+run_stream() replays a request stream in real time against a server;
+run_stream_fp64() serves the same stream with the plain FP64 engine, one
+request at a time, as the comparison point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .engine import FIELD_IDS, AerofluxError, Config, New
+
+
+class Server:
+    def __init__(self, budget_bytes: int, max_slots: int = 32, device: int = 0, max_round_steps: int = 4,
+                 retain: bool = False, max_resident_cells: int = 0):
+        h = C.c_void_p()
+        buf = C.create_string_buffer(512)
+        rc = L.lib().af_server_create(budget_bytes, max_slots, max_resident_cells, device, max_round_steps,
+                                      int(retain), C.byref(h), buf, 512)
+        if rc != L.AF_OK:
+            raise AerofluxError(buf.value.decode(), rc)
+        self._h = h
+
+    def _check(self, rc):
+        if rc != L.AF_OK:
+            raise AerofluxError((L.lib().af_server_last_error(self._h) or b"").decode(), rc)
+
+    def now(self) -> float:
+        t = C.c_double()
+        self._check(L.lib().af_server_now(self._h, C.byref(t)))
+        return t.value
+
+    def submit(self, cfg: Config, steps: int, seed: int = 42, arrival: float = -1.0) -> int:
+        i = C.c_int64()
+        self._check(L.lib().af_server_submit(self._h, C.byref(cfg.to_c()), steps, seed, arrival, C.byref(i)))
+        return i.value
+
+    def round(self) -> tuple[int, int, int]:
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(L.lib().af_server_round(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def results(self) -> list[dict]:
+        buf = (L.AfRequestResult * 256)()
+        out = []
+        while True:
+            n = C.c_int64()
+            self._check(L.lib().af_server_results(self._h, buf, 256, C.byref(n)))
+            for k in range(n.value):
+                r = buf[k]
+                out.append({f: getattr(r, f) for f, _ in L.AfRequestResult._fields_ if f != "reserved"})
+            if n.value < 256:
+                return out
+
+    def download(self, rid: int, name: str, count: int) -> np.ndarray:
+        a = np.empty(count)
+        self._check(L.lib().af_server_download(self._h, rid, FIELD_IDS[name], a.ctypes.data, count))
+        return a
+
+    def release(self, rid: int) -> None:
+        self._check(L.lib().af_server_release(self._h, rid))
+
+    def stats(self) -> dict:
+        s = L.AfServerStats()
+        self._check(L.lib().af_server_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in L.AfServerStats._fields_}
+
+    def tune(self, reps: int = 3) -> str:
+        buf = C.create_string_buffer(1 << 16)
+        self._check(L.lib().af_server_tune(self._h, reps, buf, 1 << 16))
+        return buf.value.decode()
+
+    def close(self):
+        if self._h:
+            L.lib().af_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _summary(done: list[dict], window: float, offered_cell_steps: float, n_offered: int) -> dict:
+    lat = np.array([r["completed_s"] - r["arrival_s"] for r in done]) if done else np.array([np.nan])
+    served = float(sum(r["cells"] * r["steps"] for r in done))
+    return {"window_s": window, "offered_requests": n_offered, "completed_requests": len(done),
+            "p50_latency_s": float(np.percentile(lat, 50)) if done else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if done else None,
+            "completed_cell_steps_per_s": served / window,
+            "offered_cell_steps_per_s": offered_cell_steps / window,
+            "worst_max_divergence": float(max((r["max_divergence"] for r in done), default=float("nan")))}
+
+
+def run_stream(requests, window: float, budget_bytes: int = 150 << 30, max_slots: int = 64,
+               max_round_steps: int = 4, device: int = 0, tune_after: int = 8,
+               max_resident_cells: int = 24 << 20) -> dict:
+    """Replays (arrival_s, cfg, steps) in real time for `window` seconds."""
+    srv = Server(budget_bytes, max_slots, device, max_round_steps, max_resident_cells=max_resident_cells)
+    pending = [r for r in requests if r[0] < window]
+    offered = sum(c.NX * c.NY * c.NZ * s for _, c, s in pending)
+    i, done, tuned = 0, [], False
+    t0 = srv.now()
+    while True:
+        now = srv.now() - t0
+        if now >= window:
+            break
+        while i < len(pending) and pending[i][0] <= now:
+            a, cfg, steps = pending[i]
+            srv.submit(cfg, steps, seed=42, arrival=t0 + a)
+            i += 1
+        fin, resident, queued = srv.round()
+        if not tuned and (resident >= min(tune_after, max_slots) or srv.stats()["used_bytes"] > 0 and queued > 0):
+            srv.tune(2)
+            tuned = True
+        done += [r for r in srv.results() if r["completed_s"] - t0 <= window]
+        if resident == 0 and queued == 0 and i < len(pending):
+            time.sleep(max(0.0, min(0.01, pending[i][0] - (srv.now() - t0))))
+    st = srv.stats()
+    srv.close()
+    for r in done:
+        r["arrival_s"] -= t0
+        r["completed_s"] -= t0
+        r["admitted_s"] -= t0
+    out = _summary(done, window, offered, len(pending))
+    out.update({"executed_cell_steps_per_s": st["executed_cell_steps"] / window, "queued_at_end": st["queued"],
+                "resident_at_end": st["resident"], "max_slots": max_slots, "budget_bytes": budget_bytes,
+                "max_resident_cells": max_resident_cells, "tuned": tuned})
+    return out
+
+
+def run_stream_fp64(requests, window: float, device: int = 0, chunk: int = 10) -> dict:
+    """The same stream served one request at a time by the plain FP64 engine
+    (GaussSeidelIters at its default)."""
+    pending = [r for r in requests if r[0] < window]
+    offered = sum(c.NX * c.NY * c.NZ * s for _, c, s in pending)
+    done = []
+    t0 = time.perf_counter()
+    for rid, (arrival, cfg, steps) in enumerate(pending, start=1):
+        now = time.perf_counter() - t0
+        if now >= window:
+            break
+        if arrival > now:
+            time.sleep(arrival - now)
+        c = Config(**{k: getattr(cfg, k) for k in ("NX", "NY", "NZ", "H", "DT", "Viscosity", "Density")},
+                   Device=device)
+        e = New(c)
+        e.SeedDevice(1.0, 0.01, 42, rid)
+        e.applyVelocityBC()
+        left = steps
+        while left > 0 and time.perf_counter() - t0 < window:
+            k = min(chunk, left)
+            e.Step(k)
+            left -= k
+        md = e.MaxDivergence()
+        e.Close()
+        t = time.perf_counter() - t0
+        if left == 0 and t <= window:
+            done.append({"cells": cfg.NX * cfg.NY * cfg.NZ, "steps": steps, "arrival_s": arrival, "completed_s": t,
+                         "max_divergence": md})
+    return _summary(done, window, offered, len(pending))

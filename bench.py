@@ -254,6 +254,107 @@ def device_timed(e, steps: int, warmup: int, dist, clocks=None):
             "launches": prof.kernel_launches, "rbgs_launches": prof.rbgs_launches, "passes": passes, "clocks": clk}
 
 
+def bench_mixed_512(args, dist, local, rank):
+    """512^3 mixed-precision config: DT=0.0005, noise 0.05, max|div| <= 1e-10."""
+    from aeroflux_gb300 import New
+    from aeroflux_gb300.workloads import MIXED_512
+    e = New(MIXED_512.config(Device=local, DivTol=1e-10))
+    e.SeedDevice(1.0, MIXED_512.noise, 42, rank)
+    e.applyVelocityBC()
+    steps = max(2, args.steps // 2)
+    t = device_timed(e, steps, 1, dist)
+    n = MIXED_512.n ** 3
+    out = {"value": n * steps * dist.world / t["dev_s"], "unit": UNIT, "steps": steps,
+           "ms_per_step": t["dev_s"] * 1e3 / steps, "max_divergence_after": e.MaxDivergence(),
+           "refinement_passes_last_projection": t["passes"],
+           "stages_ms_per_step": {"projections": t["solve_ms"], "sweeps": t["sweep_ms"]},
+           "workload": MIXED_512.name,
+           "error_vs_converged_fp64": "stated at 16^3 in tests/test_gpu_mixed.py: 4e-13 (one projection), "
+                                      "<=5.2e-6 relative after 5 steps (binary32 advection)"}
+    e.Close()
+    return out
+
+
+def bench_batched(args, dist, local):
+    """256 uneven grids, one persistent launch per stage, one graph per step."""
+    from aeroflux_gb300 import New
+    from aeroflux_gb300.batch import Batch
+    from aeroflux_gb300.workloads import batched_instances
+    cfgs = batched_instances(256)
+    b = Batch(len(cfgs), device=local)
+    slots = [b.assign(c) for c in cfgs]
+    t0 = time.perf_counter()
+    tune = b.tune(3)
+    tune_s = time.perf_counter() - t0
+    for s in slots:
+        b.seed(s, 1.0, 0.01, 42, s)
+    b.apply_velocity_bc()
+    cells = sum(c.NX * c.NY * c.NZ for c in cfgs)
+    steps = args.steps
+    for _ in range(args.warmup):
+        b.step(1)
+    b.profile(True)
+    dev_ms = sw = pj = 0.0
+    dist.barrier()
+    for _ in range(steps):
+        b.step(1)
+        p = b.last_step_profile()
+        dev_ms += p.step_ms
+        sw += p.sweep_ms
+        pj += p.rbgs_ms
+    dev_s = dist.max(dev_ms / 1e3)
+    worst = max(b.max_divergence(s) for s in slots)
+    passes = max(b.projection_stats(s)[0] for s in slots)
+    b.close()
+    value = cells * steps * dist.world / dev_s
+    # The plain FP64 form on the same mixed-size workload: a sample of the
+    # grids, each alone (GaussSeidelIters at its default).
+    sample = cfgs[:: max(1, len(cfgs) // 16)]
+    tot_cells_steps, tot_s, divs = 0, 0.0, []
+    for i, c in enumerate(sample):
+        cf = type(c)(**{k: getattr(c, k) for k in ("NX", "NY", "NZ", "H", "DT", "Viscosity", "Density")},
+                     Device=local)
+        e = New(cf)
+        e.SeedDevice(1.0, 0.01, 42, i)
+        e.applyVelocityBC()
+        e.Step(1)
+        e.Profile(True)
+        k = 3
+        ms = 0.0
+        for _ in range(k):
+            e.Step(1)
+            ms += e.LastStepProfile().step_ms
+        tot_cells_steps += c.NX * c.NY * c.NZ * k
+        tot_s += ms / 1e3
+        divs.append(e.MaxDivergence())
+        e.Close()
+    plain = tot_cells_steps / tot_s
+    return {"value": value, "unit": UNIT, "instances": len(cfgs), "cells": cells, "steps": steps,
+            "ms_per_step": dev_s * 1e3 / steps, "stages_ms_per_step": {"sweeps": sw / steps, "projections": pj / steps},
+            "worst_max_divergence_after": worst, "max_refinement_passes_last_projection": passes,
+            "autotune_s": tune_s, "autotuned_stages": len(tune),
+            "plain_fp64_same_workload": {"value": plain, "unit": UNIT, "sample_grids": len(sample),
+                                         "worst_max_divergence_after": max(divs),
+                                         "gauss_seidel_iters": 24},
+            "speedup_vs_plain_fp64": value / plain,
+            "workload": "256 grids, extents from {32,48,64,96,128} by PCG32 seed, H=1/max, nu log-uniform "
+                        "[1e-6,1e-4], DT=min(0.004, 0.5H^2/(6nu)), mixed form, div tol 1e-10"}
+
+
+def bench_served(args, local):
+    from aeroflux_gb300.serve import run_stream, run_stream_fp64
+    from aeroflux_gb300.workloads import served_requests
+    reqs = served_requests(200.0, args.serve_seconds, 42)
+    mixed = run_stream(reqs, args.serve_seconds, budget_bytes=150 << 30, max_slots=32, max_round_steps=4,
+                       device=local)
+    fp64 = run_stream_fp64(reqs, args.serve_seconds, device=local)
+    return {"mixed": mixed, "plain_fp64_sequential": fp64,
+            "workload": f"Poisson arrivals at 200/s for {args.serve_seconds:g} s (of the 60 s stream), extents "
+                        "uniform over multiples of 16 in [32,192], steps uniform in [50,500], 150 GB budget",
+            "completed_throughput_ratio": (mixed["completed_cell_steps_per_s"] /
+                                           max(fp64["completed_cell_steps_per_s"], 1e-30))}
+
+
 def bench_ours(args):
     from aeroflux_gb300 import _lib as L
 
@@ -308,7 +409,7 @@ def bench_ours(args):
     traffic = profiled_traffic("rbgs_fp64_256")
     fma_rate = C.c_double()
     lib.af_device_fp64_rate(local, C.byref(fma_rate))
-    fp64_inst = 9 * cells / 2  # per update: 5 adds, 1 sub, and mul+2 FMA for the exact /6
+    fp64_inst = 6 * cells / 2  # per update: 5 adds and 1 subtract; the exact /6 runs on the integer pipe
     fp64_ach = fp64_inst / rb_launch_s
 
     # --- mixed precision, at 1e-10 and at the plain form's own max|div| ------
@@ -325,6 +426,14 @@ def bench_ours(args):
                         "dtype": "f32 sweeps and inner multigrid, f64 state/residual/accumulator"}
         em.Close()
 
+    extra = {}
+    if "c3" in args.legs:
+        extra["mixed_512"] = bench_mixed_512(args, dist, local, rank)
+    if "c4" in args.legs:
+        extra["batched"] = bench_batched(args, dist, local)
+    if "c5" in args.legs and world == 1:
+        extra["served"] = bench_served(args, local)
+
     dist.close()
     if rank != 0:
         return 0
@@ -340,11 +449,12 @@ def bench_ours(args):
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "fp64_pipe": {"achieved": fp64_ach, "peak": fma_rate.value, "unit": "FP64 inst/s",
                                    "frac": fp64_ach / fma_rate.value if fma_rate.value else None,
-                                   "inst_per_update": 9}},
+                                   "inst_per_update": 6}},
         "stages_ms_per_step": {"rbgs": t["solve_ms"], "sweeps": t["sweep_ms"], "step": t["dev_s"] * 1e3 / args.steps},
         "max_divergence_after": md_plain,
         "clocks": t["clocks"],
         **mixed,
+        **extra,
     })
     if world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads()
@@ -363,6 +473,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--legs", default="c3,c4,c5", help="extra measurements: c3 (512^3 mixed), c4 (batched), "
+                                                       "c5 (served)")
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -185,6 +185,12 @@ typedef struct af_step_profile {
 int af_profile(af_engine* e, int enable);
 int af_last_step_profile(af_engine* e, af_step_profile* out);
 
+/* Self-test of the red-black update's correctly rounded x/6 (the integer
+ * form the kernel uses and the FMA-remainder form) against IEEE division on
+ * n random binary64 bit patterns from `seed`; *mismatches counts differing
+ * results (NaN compared by NaN-ness). */
+int af_selftest_div6(int device, int64_t n, uint64_t seed, int64_t* mismatches);
+
 /* Measures the device's binary64 FMA issue rate (independent DFMA chains),
  * in FMA instructions per second, for the FP64 roofline. */
 int af_device_fp64_rate(int device, double* fma_per_s);
@@ -230,8 +236,64 @@ int af_batch_projection_stats(af_batch* b, int64_t slot, int64_t* passes, double
 int af_batch_tune(af_batch* b, int32_t reps, char* report, size_t len);
 int af_batch_profile(af_batch* b, int enable);
 int af_batch_last_step_profile(af_batch* b, af_step_profile* out);
+/* Writes a slot's initial field on the device: the Taylor-Green vortex of
+ * amplitude amp (binary32 sinpi/cospi) plus uniform [-noise, noise] from
+ * PCG32(seed, stream) in af_seed_taylor_green's draw order; apply the
+ * velocity BC afterwards. */
+int af_batch_seed(af_batch* b, int64_t slot, double amp, double noise, uint64_t seed, uint64_t stream);
 void af_batch_destroy(af_batch* b);
 const char* af_batch_last_error(const af_batch* b);
+
+/* ---------------------------------------------------------------------------
+ * Serving: a continuous-batching request loop over a batch (no counterpart
+ * in the reference).  Requests queue in arrival order; each round admits
+ * queued requests while a slot and enough of the device budget are free
+ * (state created by af_batch_seed and kept resident), advances every
+ * resident request by the same number of Steps (at most max_round_steps) in
+ * one batched graph launch, and retires finished requests with their
+ * max|div| read back.  A request's bits do not depend on what else is
+ * resident.  retain != 0 keeps finished requests resident (inactive) until
+ * af_server_release so their fields can be downloaded.
+ * ------------------------------------------------------------------------- */
+typedef struct af_server af_server;
+
+typedef struct af_request_result {
+    int64_t id;
+    int32_t status;            /* AF_OK or AF_ERR_FAULT */
+    int32_t reserved;
+    int64_t cells;             /* interior cells */
+    int64_t steps;             /* Steps performed */
+    int64_t refinement_passes; /* of the last projection */
+    double arrival_s, admitted_s, completed_s;  /* server clock */
+    double max_divergence;     /* MaxDivergence of the result */
+} af_request_result;
+
+typedef struct af_server_stats {
+    int64_t queued, resident, retained;
+    int64_t budget_bytes, used_bytes;
+    int64_t executed_cell_steps;
+    double now_s;
+} af_server_stats;
+
+/* max_resident_cells > 0 also caps the interior cells resident at once (the
+ * work one round advances), so under overload requests finish instead of all
+ * crawling; one request is always admitted when none is running. */
+int af_server_create(int64_t budget_bytes, int64_t max_slots, int64_t max_resident_cells, int32_t device,
+                     int32_t max_round_steps, int32_t retain, af_server** out, char* err, size_t errlen);
+/* Seconds since creation (the clock of arrival/admission/completion times). */
+int af_server_now(af_server* s, double* seconds);
+/* cfg must be MIXED; arrival_s < 0 stamps the current time. */
+int af_server_submit(af_server* s, const af_config* cfg, int64_t steps, uint64_t seed, double arrival_s, int64_t* id);
+int af_server_round(af_server* s, int64_t* completed_now, int64_t* resident, int64_t* queued);
+/* Moves up to cap finished requests' results out; *n gets how many. */
+int af_server_results(af_server* s, af_request_result* out, int64_t cap, int64_t* n);
+int af_server_download(af_server* s, int64_t id, int field, double* host, size_t count);
+int af_server_release(af_server* s, int64_t id);
+int af_server_get_stats(af_server* s, af_server_stats* out);
+/* The batch autotuner on the requests currently resident. */
+int af_server_tune(af_server* s, int32_t reps, char* report, size_t len);
+void af_server_destroy(af_server* s);
+const char* af_server_last_error(const af_server* s);
 
 /* Synthetic input (no counterpart in the reference API; its tests seed a
  * trigonometric field straight into arena views, engine_test.go:302-335).
@@ -261,6 +323,12 @@ int af_seed_taylor_green(const af_config* cfg, double amp, double noise, uint64_
  * the GPU race. */
 int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, const double* v, const double* w,
                               void* stream, double* out, char* err, size_t errlen);
+
+/* The same synthetic field written on the device (no counterpart in the
+ * reference): Taylor-Green of amplitude amp with binary32 sinpi/cospi plus
+ * uniform [-noise, noise] from PCG32(seed, stream) in af_seed_taylor_green's
+ * draw order; U, V, W and Tmp0-2 are zeroed first.  Apply the BC after. */
+int af_seed_device(af_engine* e, double amp, double noise, uint64_t seed, uint64_t stream);
 
 /* Close, aeroflux.go:419-439: release device memory.  Idempotent. */
 int af_close(af_engine* e);
