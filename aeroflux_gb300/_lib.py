@@ -92,6 +92,7 @@ SIGNATURES = {
     "af_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
     "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "af_selftest_div6": (C.c_int, [C.c_int, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
+    "af_selftest_dadd": (C.c_int, [C.c_int, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "af_batch_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.POINTER(_E), *_ERR]),
     "af_batch_slot_bytes": (C.c_int, [C.POINTER(AfConfig), C.POINTER(C.c_int64)]),
     "af_batch_assign": (C.c_int, [_E, C.POINTER(AfConfig), C.POINTER(C.c_int64)]),

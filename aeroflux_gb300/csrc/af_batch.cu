@@ -65,6 +65,7 @@ struct Lvl {
     float* e;
     float* r;
     FastDiv fnx, fny, fhx;  // nx, ny, (nx+1)/2
+    float* e2;              // second buffer of the fused red-black pair (levels below the tail)
 };
 
 struct Ctl {
@@ -87,7 +88,9 @@ struct InstDev {
     double thresh;      // 0.5 * div_tol
     unsigned max_refine;
     int nlev;
-    int coarse_sweeps;  // > 0: one-block coarse solve; 0: smoothing at the coarsest level
+    int coarse_sweeps;  // sweeps of the coarsest solve inside the tail V-cycle
+    int tail;           // first level of the one-block tail V-cycle; -1: coarsest too large, smoothed instead
+    int tail_floats;    // shared-memory floats of the tail levels (e and r)
     int parity;         // 1 when U/V/W live in the Tmp slots
     int active;
     FastDiv fpx, fpy;        // padded P extents
@@ -103,7 +106,8 @@ enum {
     S_RESTRICT = S_SMOOTH + kMaxLev,
     S_PROLONG = S_RESTRICT + kMaxLev,
     S_BIGCOARSE = S_PROLONG + kMaxLev,
-    S_COUNT = S_BIGCOARSE + kMaxLev
+    S_PAIR = S_BIGCOARSE + kMaxLev,
+    S_COUNT = S_PAIR + kMaxLev
 };
 
 struct Shape {
@@ -391,6 +395,28 @@ __device__ __forceinline__ long long lidx(int x, int y, int z, int nx, int ny) {
     return x + (long long)nx * (y + (long long)ny * z);
 }
 
+// Binary32 cell formulas of the multigrid with every rounding written out
+// (no contraction left to the compiler), so the per-level kernels, the fused
+// red-black pair and the one-block tail V-cycle compute the same bits.
+// Relaxation of one cell: (wx*sx + wy*sy + wz*sz - r) / (2*(wx+wy+wz)).
+__device__ __forceinline__ float mg_relax(const Lvl& L, float sx, float sy, float sz, float r, float inv) {
+    return __fmul_rn(__fsub_rn(__fmaf_rn(L.wz, sz, __fmaf_rn(L.wy, sy, __fmul_rn(L.wx, sx))), r), inv);
+}
+// Residual of one cell: r - (wx*dxx + wy*dyy + wz*dzz), d** the second differences.
+__device__ __forceinline__ float mg_res(const Lvl& L, float sx, float sy, float sz, float c, float r) {
+    const float c2 = 2.0f * c;
+    return __fsub_rn(r, __fmaf_rn(L.wz, __fsub_rn(sz, c2), __fmaf_rn(L.wy, __fsub_rn(sy, c2), __fmul_rn(L.wx, __fsub_rn(sx, c2)))));
+}
+// Trilinear weights (a* on the parent, b* = 1 - a* on its neighbour).
+__device__ __forceinline__ float mg_interp(float ax, float ay, float az, float e000, float e100, float e010, float e110,
+                                           float e001, float e101, float e011, float e111) {
+    const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
+    auto lx = [&](float p, float q) { return __fmaf_rn(bx, q, __fmul_rn(ax, p)); };
+    auto ly = [&](float p, float q) { return __fmaf_rn(by, q, __fmul_rn(ay, p)); };
+    const float z0 = ly(lx(e000, e100), lx(e010, e110)), z1 = ly(lx(e001, e101), lx(e011, e111));
+    return __fmaf_rn(bz, z1, __fmul_rn(az, z0));
+}
+
 __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color) {
     FOR_TILES(tab)
     if (ctl[s].stopped) continue;
@@ -410,7 +436,7 @@ __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, i
         const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c);
         const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c);
         const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c);
-        L.e[i] = (L.wx * sx + L.wy * sy + L.wz * sz - L.r[i]) * inv;
+        L.e[i] = mg_relax(L, sx, sy, sz, L.r[i], inv);
     }
     END_ELEMS
     END_TILES
@@ -420,10 +446,10 @@ __device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) 
     const long long nxy = (long long)L.nx * L.ny;
     const long long i = lidx(x, y, z, L.nx, L.ny);
     const float c = L.e[i];
-    const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c) - 2.0f * c;
-    const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c) - 2.0f * c;
-    const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c) - 2.0f * c;
-    return L.r[i] - (L.wx * sx + L.wy * sy + L.wz * sz);
+    const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c);
+    const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c);
+    const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c);
+    return mg_res(L, sx, sy, sz, c, L.r[i]);
 }
 
 // Coarse rhs = mean of the children's residuals; coarse solution = 0.
@@ -468,10 +494,8 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l) 
     if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
     if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
     auto E = [&](int i, int j, int k) { return C.e[lidx(i, j, k, C.nx, C.ny)]; };
-    const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
-    const float v = az * (ay * (ax * E(X0, Y0, Z0) + bx * E(X1, Y0, Z0)) + by * (ax * E(X0, Y1, Z0) + bx * E(X1, Y1, Z0))) +
-                    bz * (ay * (ax * E(X0, Y0, Z1) + bx * E(X1, Y0, Z1)) + by * (ax * E(X0, Y1, Z1) + bx * E(X1, Y1, Z1)));
-    F.e[el] += v;
+    F.e[el] = __fadd_rn(F.e[el], mg_interp(ax, ay, az, E(X0, Y0, Z0), E(X1, Y0, Z0), E(X0, Y1, Z0), E(X1, Y1, Z0),
+                                           E(X0, Y0, Z1), E(X1, Y0, Z1), E(X0, Y1, Z1), E(X1, Y1, Z1)));
     END_ELEMS
     END_TILES
 }
@@ -493,47 +517,201 @@ __device__ float block_sum(float v, float* red) {
     return s;
 }
 
-// Coarsest level of one slot per block: remove the mean of r (a Neumann
-// problem is solvable only for zero-mean data), red-black sweeps from zero
-// in shared memory, remove the mean of e.  Sums use a fixed tree.
-__global__ void __launch_bounds__(kCoarseThreads) kb_coarse(const InstDev* inst, const Ctl* ctl, Tab tab) {
-    __shared__ float se[kCoarseMax];
-    __shared__ float sr[kCoarseMax];
+// --- fused red-black pair ---------------------------------------------------
+// One red sweep then one black sweep of L e = r, from e_in into e_out: the
+// red values read only e_in (their black neighbours are unchanged by the red
+// sweep), the black values read the new red values, which each block
+// computes for its x-y tile plus a one-cell halo into a ring of three planes
+// while it marches over a chunk of z-planes (the chunk's first red plane and
+// the one below it are recomputed).  Nothing reads what the kernel writes, so
+// blocks never race and the result equals the two in-place colour sweeps.
+constexpr int kPairTX = 32, kPairTY = 8, kPairZC = 32;
+
+__global__ void __launch_bounds__(kPairTX * kPairTY) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab,
+                                                                    int l, int dir) {
+    __shared__ float ring[3][kPairTY + 2][kPairTX + 2];
+    const int tid = threadIdx.x + kPairTX * threadIdx.y;
+    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
+        const int s = find_slot(tab.prefix, tab.n, item);
+        if (ctl[s].stopped) continue;
+        const Lvl L = inst[s].lev[l];
+        const float* __restrict__ ein = dir ? L.e2 : L.e;
+        float* __restrict__ eout = dir ? L.e : L.e2;
+        const float* __restrict__ r = L.r;
+        const int ntx = (L.nx + kPairTX - 1) / kPairTX, nty = (L.ny + kPairTY - 1) / kPairTY;
+        int local = item - tab.prefix[s];
+        const int bx = local % ntx;
+        local /= ntx;
+        const int by = local % nty;
+        const int bz = local / nty;
+        const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairZC;
+        const int z1 = min(z0 + kPairZC, L.nz);
+        const long long nxy = (long long)L.nx * L.ny;
+        const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
+        auto red_plane = [&](int z, float (*dst)[kPairTX + 2]) {
+            for (int q = tid; q < (kPairTX + 2) * (kPairTY + 2); q += kPairTX * kPairTY) {
+                const int hx = q % (kPairTX + 2), hy = q / (kPairTX + 2);
+                const int x = x0 - 1 + hx, y = y0 - 1 + hy;
+                float v = 0.0f;
+                if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && ((x + y + z) & 1) == 0) {
+                    const long long i = x + (long long)L.nx * y + nxy * z;
+                    const float c = ein[i];
+                    const float sx = (x > 0 ? ein[i - 1] : c) + (x < L.nx - 1 ? ein[i + 1] : c);
+                    const float sy = (y > 0 ? ein[i - L.nx] : c) + (y < L.ny - 1 ? ein[i + L.nx] : c);
+                    const float sz = (z > 0 ? ein[i - nxy] : c) + (z < L.nz - 1 ? ein[i + nxy] : c);
+                    v = mg_relax(L, sx, sy, sz, r[i], inv);
+                }
+                dst[hy][hx] = v;
+            }
+        };
+        if (z0 > 0) red_plane(z0 - 1, ring[(z0 + 2) % 3]);
+        red_plane(z0, ring[z0 % 3]);
+        for (int z = z0; z < z1; ++z) {
+            if (z + 1 < L.nz) red_plane(z + 1, ring[(z + 1) % 3]);
+            __syncthreads();
+            const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+            if (x < L.nx && y < L.ny) {
+                const int hx = threadIdx.x + 1, hy = threadIdx.y + 1;
+                const long long i = x + (long long)L.nx * y + nxy * z;
+                const float(*cp)[kPairTX + 2] = ring[z % 3];
+                float out;
+                if (((x + y + z) & 1) == 0) {
+                    out = cp[hy][hx];
+                } else {
+                    const float c = ein[i];
+                    const float sx = (x > 0 ? cp[hy][hx - 1] : c) + (x < L.nx - 1 ? cp[hy][hx + 1] : c);
+                    const float sy = (y > 0 ? cp[hy - 1][hx] : c) + (y < L.ny - 1 ? cp[hy + 1][hx] : c);
+                    const float sz = (z > 0 ? ring[(z + 2) % 3][hy][hx] : c) + (z < L.nz - 1 ? ring[(z + 1) % 3][hy][hx] : c);
+                    out = mg_relax(L, sx, sy, sz, r[i], inv);
+                }
+                eout[i] = out;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// --- tail V-cycle: every level from the slot's tail down, in one block -------
+// Levels of at most kCoarseMax cells live in shared memory: pre-smoothing and
+// restriction down to the coarsest level, its solve (the mean of r removed --
+// a Neumann problem is solvable only for zero-mean data -- red-black sweeps
+// from zero, the mean of e removed), then prolongation and post-smoothing
+// back up.  Sums use a fixed tree.  Replaces one launch per level and sweep.
+__device__ void sm_smooth(const Lvl& L, float* e, const float* r, int color) {
+    const int n = L.nx * L.ny * L.nz, nxy = L.nx * L.ny;
+    const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned q = L.fnx.div((unsigned)i), zz = L.fny.div(q);
+        const int x = i - (int)q * L.nx, y = (int)q - (int)zz * L.ny, z = (int)zz;
+        if (((x + y + z) & 1) != color) continue;
+        const float c = e[i];
+        const float sx = (x > 0 ? e[i - 1] : c) + (x < L.nx - 1 ? e[i + 1] : c);
+        const float sy = (y > 0 ? e[i - L.nx] : c) + (y < L.ny - 1 ? e[i + L.nx] : c);
+        const float sz = (z > 0 ? e[i - nxy] : c) + (z < L.nz - 1 ? e[i + nxy] : c);
+        e[i] = mg_relax(L, sx, sy, sz, r[i], inv);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float sm_res(const Lvl& L, const float* e, const float* r, int x, int y, int z) {
+    const int nxy = L.nx * L.ny;
+    const int i = x + L.nx * y + nxy * z;
+    const float c = e[i];
+    const float sx = (x > 0 ? e[i - 1] : c) + (x < L.nx - 1 ? e[i + 1] : c);
+    const float sy = (y > 0 ? e[i - L.nx] : c) + (y < L.ny - 1 ? e[i + L.nx] : c);
+    const float sz = (z > 0 ? e[i - nxy] : c) + (z < L.nz - 1 ? e[i + nxy] : c);
+    return mg_res(L, sx, sy, sz, c, r[i]);
+}
+
+__global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, const Ctl* ctl, Tab tab, int nu) {
+    extern __shared__ float tsm[];
     __shared__ float red[32];
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (ctl[s].stopped) continue;
         const InstDev& I = inst[s];
-        const Lvl L = I.lev[I.nlev - 1];
-        const int n = L.nx * L.ny * L.nz;
-        float part = 0.0f;
-        for (int i = threadIdx.x; i < n; i += kCoarseThreads) {
-            sr[i] = L.r[i];
-            se[i] = 0.0f;
-            part += sr[i];
+        const int t = I.tail, nl = I.nlev;
+        float* E[kMaxLev];
+        float* R[kMaxLev];
+        {
+            float* p = tsm;
+            for (int l = t; l < nl; ++l) {
+                const int n = lvl_cells(I.lev[l]);
+                E[l] = p;
+                R[l] = p + n;
+                p += 2 * n;
+            }
         }
-        const float mean_r = block_sum(part, red) / (float)n;
-        for (int i = threadIdx.x; i < n; i += kCoarseThreads) sr[i] -= mean_r;
+        const Lvl T = I.lev[t];
+        for (int i = threadIdx.x; i < lvl_cells(T); i += blockDim.x) {
+            E[t][i] = T.e[i];
+            R[t][i] = T.r[i];
+        }
         __syncthreads();
-        const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        const int nxy = L.nx * L.ny;
-        for (int it = 0; it < 2 * I.coarse_sweeps; ++it) {
-            const int color = it & 1;
-            for (int i = threadIdx.x; i < n; i += kCoarseThreads) {
-                const int x = i % L.nx, y = (i / L.nx) % L.ny, z = i / nxy;
-                if (((x + y + z) & 1) != color) continue;
-                const float c = se[i];
-                const float sx = (x > 0 ? se[i - 1] : c) + (x < L.nx - 1 ? se[i + 1] : c);
-                const float sy = (y > 0 ? se[i - L.nx] : c) + (y < L.ny - 1 ? se[i + L.nx] : c);
-                const float sz = (z > 0 ? se[i - nxy] : c) + (z < L.nz - 1 ? se[i + nxy] : c);
-                se[i] = (L.wx * sx + L.wy * sy + L.wz * sz - sr[i]) * inv;
+        for (int l = t; l + 1 < nl; ++l) {
+            const Lvl F = I.lev[l], C = I.lev[l + 1];
+            for (int k = 0; k < nu; ++k) {
+                sm_smooth(F, E[l], R[l], 0);
+                sm_smooth(F, E[l], R[l], 1);
+            }
+            const int ex = F.cx ? 2 : 1, ey = F.cy ? 2 : 1, ez = F.cz ? 2 : 1;
+            const float inv = 1.0f / (float)(ex * ey * ez);
+            for (int j = threadIdx.x; j < lvl_cells(C); j += blockDim.x) {
+                const unsigned q = C.fnx.div((unsigned)j), zz = C.fny.div(q);
+                const int X = j - (int)q * C.nx, Y = (int)q - (int)zz * C.ny, Z = (int)zz;
+                float sum = 0.0f;
+                for (int dz = 0; dz < ez; ++dz)
+                    for (int dy = 0; dy < ey; ++dy)
+                        for (int dx = 0; dx < ex; ++dx) sum += sm_res(F, E[l], R[l], X * ex + dx, Y * ey + dy, Z * ez + dz);
+                R[l + 1][j] = sum * inv;
+                E[l + 1][j] = 0.0f;
             }
             __syncthreads();
         }
-        part = 0.0f;
-        for (int i = threadIdx.x; i < n; i += kCoarseThreads) part += se[i];
-        const float mean_e = block_sum(part, red) / (float)n;
-        for (int i = threadIdx.x; i < n; i += kCoarseThreads) L.e[i] = se[i] - mean_e;
+        {  // coarsest solve
+            const Lvl C = I.lev[nl - 1];
+            const int n = lvl_cells(C);
+            float part = 0.0f;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) part += R[nl - 1][i];
+            const float mean_r = block_sum(part, red) / (float)n;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                R[nl - 1][i] -= mean_r;
+                E[nl - 1][i] = 0.0f;
+            }
+            __syncthreads();
+            for (int k = 0; k < I.coarse_sweeps; ++k) {
+                sm_smooth(C, E[nl - 1], R[nl - 1], 0);
+                sm_smooth(C, E[nl - 1], R[nl - 1], 1);
+            }
+            part = 0.0f;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) part += E[nl - 1][i];
+            const float mean_e = block_sum(part, red) / (float)n;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) E[nl - 1][i] -= mean_e;
+            __syncthreads();
+        }
+        for (int l = nl - 2; l >= t; --l) {
+            const Lvl F = I.lev[l], C = I.lev[l + 1];
+            for (int i = threadIdx.x; i < lvl_cells(F); i += blockDim.x) {
+                const unsigned q = F.fnx.div((unsigned)i), zz = F.fny.div(q);
+                const int x = i - (int)q * F.nx, y = (int)q - (int)zz * F.ny, z = (int)zz;
+                int X0 = x, X1 = x, Y0 = y, Y1 = y, Z0 = z, Z1 = z;
+                float ax = 1.0f, ay = 1.0f, az = 1.0f;
+                if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
+                if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
+                if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
+                const float* ec = E[l + 1];
+                auto Ev = [&](int a, int b, int c) { return ec[a + C.nx * (b + C.ny * c)]; };
+                E[l][i] = __fadd_rn(E[l][i], mg_interp(ax, ay, az, Ev(X0, Y0, Z0), Ev(X1, Y0, Z0), Ev(X0, Y1, Z0),
+                                                       Ev(X1, Y1, Z0), Ev(X0, Y0, Z1), Ev(X1, Y0, Z1), Ev(X0, Y1, Z1),
+                                                       Ev(X1, Y1, Z1)));
+            }
+            __syncthreads();
+            for (int k = 0; k < nu; ++k) {
+                sm_smooth(F, E[l], R[l], 0);
+                sm_smooth(F, E[l], R[l], 1);
+            }
+        }
+        for (int i = threadIdx.x; i < lvl_cells(T); i += blockDim.x) T.e[i] = E[t][i];
         __syncthreads();
     }
 }
@@ -683,6 +861,12 @@ struct Batch {
     int grid_sz[S_COUNT] = {};       // blocks per stage, fixed when the graph is captured
     int graph_levels = 0;            // levels the captured graph covers
     unsigned graph_big = 0;          // levels whose large-coarsest smoothing the graph carries
+    unsigned graph_pair = 0;         // levels with fused-pair smoothing in the graph
+    unsigned graph_single = 0;       // levels with in-place colour sweeps in the graph
+    size_t tail_smem = 0;            // dynamic shared memory of the tail V-cycle
+    int graph_nu = 0;                // smoothing sweeps the captured graph carries
+    bool per_level = false;          // multigrid without the tail V-cycle above the coarsest level
+    bool pairs = false;              // fused red-black pair smoothing below the tail
     cudaGraphExec_t graph = nullptr;
     bool tables_dirty = true;
     bool profiling = false;
@@ -708,7 +892,26 @@ int max_levels(const Batch* b) {
 unsigned big_coarse_levels(const Batch* b) {
     unsigned m = 0;
     for (const auto& s : b->slots)
-        if (s.used && s.d.coarse_sweeps == 0) m |= 1u << (s.d.nlev - 1);
+        if (s.used && s.d.tail < 0) m |= 1u << (s.d.nlev - 1);
+    return m;
+}
+
+// Levels some slot smooths with fused pairs (pair = true) or in place.
+unsigned smooth_levels(const Batch* b, bool pair) {
+    unsigned m = 0;
+    for (const auto& s : b->slots) {
+        if (!s.used) continue;
+        const int lim = s.d.tail >= 0 ? s.d.tail : s.d.nlev - 1;
+        for (int l = 0; l < lim; ++l)
+            if ((s.d.lev[l].e2 != nullptr) == pair) m |= 1u << l;
+    }
+    return m;
+}
+
+size_t tail_smem_bytes(const Batch* b) {
+    size_t m = 0;
+    for (const auto& s : b->slots)
+        if (s.used && s.d.tail >= 0) m = std::max(m, (size_t)s.d.tail_floats * sizeof(float));
     return m;
 }
 
@@ -723,19 +926,27 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
     else if (st == S_PBC) n = pbc_count(I.g);
-    else if (st == S_COARSE) return I.coarse_sweeps > 0 ? 1 : 0;
-    else if (st >= S_SMOOTH && st < S_RESTRICT) {
+    else if (st == S_COARSE) return I.tail >= 0 ? 1 : 0;
+    const int lim = I.tail >= 0 ? I.tail : I.nlev - 1;  // levels smoothed by per-level kernels
+    if (st < S_SMOOTH) {
+        // n set above
+    } else if (st < S_RESTRICT) {
         const int l = st - S_SMOOTH;
-        n = l < I.nlev - 1 ? half_box(I.lev[l]) : 0;
+        n = (l < lim && !I.lev[l].e2) ? half_box(I.lev[l]) : 0;
     } else if (st >= S_RESTRICT && st < S_PROLONG) {
         const int l = st - S_RESTRICT;
-        n = l < I.nlev - 1 ? lvl_cells(I.lev[l + 1]) : 0;
+        n = l < lim ? lvl_cells(I.lev[l + 1]) : 0;
     } else if (st >= S_PROLONG && st < S_BIGCOARSE) {
         const int l = st - S_PROLONG;
-        n = l < I.nlev - 1 ? lvl_cells(I.lev[l]) : 0;
-    } else {
+        n = l < lim ? lvl_cells(I.lev[l]) : 0;
+    } else if (st >= S_BIGCOARSE && st < S_PAIR) {
         const int l = st - S_BIGCOARSE;
-        n = (l == I.nlev - 1 && I.coarse_sweeps == 0) ? half_box(I.lev[l]) : 0;
+        n = (l == I.nlev - 1 && I.tail < 0) ? half_box(I.lev[l]) : 0;
+    } else if (st >= S_PAIR && st < S_COUNT) {
+        const int l = st - S_PAIR;
+        if (l >= lim || !I.lev[l].e2) return 0;
+        const Lvl& L = I.lev[l];
+        return cdivl(L.nx, kPairTX) * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairZC);
     }
     return cdivl(n, per);
 }
@@ -808,18 +1019,32 @@ void enq_smooth(Batch* b, int st, int l, int pairs, cudaStream_t s) {
     }
 }
 
+// Pre- or post-smoothing of level l: fused pairs ping-ponging through e2
+// (an even count returns the result to e) for slots that have e2, in-place
+// colour sweeps for the others.
+void enq_level_smooth(Batch* b, int l, cudaStream_t s) {
+    if (b->graph_pair & (1u << l))
+        for (int k = 0; k < b->nu; ++k) {
+            kb_smooth_pair<<<grid(b, S_PAIR + l), dim3(kPairTX, kPairTY), 0, s>>>(b->d_inst, b->d_ctl,
+                                                                                tab(b, S_PAIR + l), l, k & 1);
+            ++b->launches;
+        }
+    if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+}
+
 void enq_vcycle(Batch* b, cudaStream_t s) {
     const int L = b->graph_levels;
     for (int l = 0; l + 1 < L; ++l) {
-        enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+        enq_level_smooth(b, l, s);
         LAUNCH(b, S_RESTRICT + l, kb_restrict, b->d_inst, b->d_ctl, tab(b, S_RESTRICT + l), l);
     }
-    LAUNCH(b, S_COARSE, kb_coarse, b->d_inst, b->d_ctl, tab(b, S_COARSE));
+    kb_vtail<<<grid(b, S_COARSE), kCoarseThreads, b->tail_smem, s>>>(b->d_inst, b->d_ctl, tab(b, S_COARSE), b->nu);
+    ++b->launches;
     for (int l = 0; l < L; ++l)
         if (b->graph_big & (1u << l)) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, s);
     for (int l = L - 2; l >= 0; --l) {
         LAUNCH(b, S_PROLONG + l, kb_prolong, b->d_inst, b->d_ctl, tab(b, S_PROLONG + l), l);
-        enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+        enq_level_smooth(b, l, s);
     }
 }
 
@@ -937,14 +1162,21 @@ cudaError_t prepare(Batch* b) {
     cudaError_t rc;
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     const int L = max_levels(b);
-    const unsigned big = big_coarse_levels(b);
-    if (b->graph && (L > b->graph_levels || (big & ~b->graph_big))) {
+    const unsigned big = big_coarse_levels(b), pair = smooth_levels(b, true), single = smooth_levels(b, false);
+    const size_t tsm = tail_smem_bytes(b);
+    if (b->graph && (L > b->graph_levels || (big & ~b->graph_big) || (pair & ~b->graph_pair) ||
+                     (single & ~b->graph_single) || tsm > b->tail_smem || b->graph_nu != b->nu)) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
     if (!b->graph) {
         b->graph_levels = std::max(L, b->graph_levels);
         b->graph_big |= big;
+        b->graph_pair |= pair;
+        b->graph_single |= single;
+        b->tail_smem = std::max(b->tail_smem, tsm);
+        b->graph_nu = b->nu;
+        cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem);
         b->launches = 0;
         size_grids(b);
         if ((rc = capture(b, [&] { enq_step(b, b->stream); }, &b->graph)) != cudaSuccess) {
@@ -975,8 +1207,13 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
     if (const char* fp = getenv("AEROFLUX_FIXED_REFINEMENT_PASSES")) b->fixed_passes = std::max(0, atoi(fp));
+    // Per-level multigrid kernels only (no tail V-cycle above the coarsest
+    // level), and fused red-black pairs on or off: the same bits either way.
+    if (const char* pl = getenv("AEROFLUX_MG_PER_LEVEL")) b->per_level = atoi(pl) != 0;
+    if (const char* fp = getenv("AEROFLUX_MG_PAIRS")) b->pairs = atoi(fp) != 0;
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
+    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{kPairTX * kPairTY, 1, 8};
     cudaError_t rc;
     if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -1045,13 +1282,20 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
         if (cz) { nz /= 2; wz *= 0.25f; }
     }
     const Lvl& last = lev[n - 1];
-    if (lvl_cells(last) > kCoarseMax) {
-        *coarse_sweeps = 0;  // smoothing in place of a coarse solve
-    } else {
-        const int nmax = std::max(last.nx, std::max(last.ny, last.nz));
-        *coarse_sweeps = std::min(1000, std::max(8, 2 * nmax * nmax));
-    }
+    const int nmax = std::max(last.nx, std::max(last.ny, last.nz));
+    *coarse_sweeps = std::min(1000, std::max(8, 2 * nmax * nmax));
     return n;
+}
+
+// First level of the one-block tail V-cycle (every level from it down has at
+// most kCoarseMax cells), or -1 when the coarsest level is larger.
+int plan_tail(const Lvl* lev, int n, int* floats, bool coarsest_only = false) {
+    *floats = 0;
+    if (lvl_cells(lev[n - 1]) > kCoarseMax) return -1;
+    int t = n - 1;
+    while (!coarsest_only && t > 0 && lvl_cells(lev[t - 1]) <= kCoarseMax) --t;
+    for (int l = t; l < n; ++l) *floats += 2 * (int)lvl_cells(lev[l]);
+    return t;
 }
 
 af_field_desc fdesc(int64_t* off, int64_t nx, int64_t ny, int64_t nz) {
@@ -1082,10 +1326,12 @@ size_t batch_slot_bytes(const af_config& c) {
     const size_t arena = ((size_t)off + 255) & ~(size_t)255;
     const size_t bb = ((size_t)(cx * cy * cz) * 8 + 255) & ~(size_t)255;
     Lvl lev[kMaxLev];
-    int cs = 0;
+    int cs = 0, tf = 0;
     const int nl = plan_levels((int)c.nx, (int)c.ny, (int)c.nz, lev, &cs);
+    const int tail = plan_tail(lev, nl, &tf);
+    const int lim = tail >= 0 ? tail : nl - 1;
     size_t mg = 0;
-    for (int l = 0; l < nl; ++l) mg += 2 * (size_t)lvl_cells(lev[l]) * sizeof(float);
+    for (int l = 0; l < nl; ++l) mg += ((l < lim && c.inner_sweeps % 2 == 0) ? 3 : 2) * (size_t)lvl_cells(lev[l]) * sizeof(float);
     return arena + bb + ((mg + 255) & ~(size_t)255);
 }
 
@@ -1137,10 +1383,22 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.fnx = FastDiv((unsigned)I.g.NX);
     I.fny = FastDiv((unsigned)I.g.NY);
     I.nlev = plan_levels(I.g.NX, I.g.NY, I.g.NZ, I.lev, &I.coarse_sweeps);
+    I.tail = plan_tail(I.lev, I.nlev, &I.tail_floats, b->per_level);
+    const int lim = I.tail >= 0 ? I.tail : I.nlev - 1;
+    // Fused red-black pairs need an even sweep count (the ping-pong returns
+    // the result to e) and run on every level below the tail.  The batch's
+    // sweep count is the first slot's; a slot joining a batch that sweeps an
+    // odd number of times smooths in place.
+    bool others = false;
+    for (int i = 0; i < b->cap; ++i)
+        if (i != s && b->slots[i].used) others = true;
+    const int batch_nu = others ? b->nu : (int)c.inner_sweeps;
+    const bool fused = c.inner_sweeps % 2 == 0 && batch_nu % 2 == 0 && b->pairs;
     const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
     const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
     size_t mg = 0;
-    for (int l = 0; l < I.nlev; ++l) mg += 2 * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
+    for (int l = 0; l < I.nlev; ++l)
+        mg += ((l < lim && fused) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
     mg = (mg + 255) & ~(size_t)255;
     S.external_arena = arena != nullptr;
     S.mem_bytes = (arena ? 0 : arena_bytes) + b_bytes + mg;
@@ -1169,9 +1427,15 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     p += b_bytes;
     float* fp = (float*)p;
     for (int l = 0; l < I.nlev; ++l) {
+        const long long n = lvl_cells(I.lev[l]);
         I.lev[l].e = fp;
-        I.lev[l].r = fp + lvl_cells(I.lev[l]);
-        fp += 2 * lvl_cells(I.lev[l]);
+        I.lev[l].r = fp + n;
+        fp += 2 * n;
+        I.lev[l].e2 = nullptr;
+        if (l < lim && fused) {
+            I.lev[l].e2 = fp;
+            fp += n;
+        }
     }
     cudaMemsetAsync(p, 0, mg, b->stream);
     const double half = c.dt * 0.5;  // aeroflux.go:353
@@ -1187,10 +1451,7 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.parity = 0;
     // Smoothing sweeps per level are a property of the batch's step graph:
     // the first slot of an empty batch sets them.
-    bool empty = true;
-    for (int i = 0; i < b->cap; ++i)
-        if (i != s && b->slots[i].used) empty = false;
-    if (empty) b->nu = (int)c.inner_sweeps;
+    b->nu = batch_nu;
     S.used = true;
     S.active = true;
     b->tables_dirty = true;
@@ -1250,6 +1511,10 @@ cudaError_t batch_project(Batch* b, std::string* err) {
     }
     b->graph_levels = std::max(b->graph_levels, max_levels(b));
     b->graph_big |= big_coarse_levels(b);
+    b->graph_pair |= smooth_levels(b, true);
+    b->graph_single |= smooth_levels(b, false);
+    b->tail_smem = std::max(b->tail_smem, tail_smem_bytes(b));
+    cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem);
     size_grids(b);
     cudaGraphExec_t g = nullptr;
     const bool prof = b->profiling;

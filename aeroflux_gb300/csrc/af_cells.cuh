@@ -66,6 +66,61 @@ __device__ __forceinline__ double div6_int(double x) {
     return __longlong_as_double((long long)((b & kSign) | (e << 52) | (Q & 0xFFFFFFFFFFFFFull)));
 }
 
+// RN(a + b) in binary64 on the integer pipe.  Significands are aligned in
+// 64-bit integers with the leading bit at 62, leaving 10 guard bits; bits
+// shifted out of the smaller operand fold into a sticky bit.  Equal signs
+// add (one carry renormalisation), opposite signs subtract and renormalise
+// left (exact whenever more than the guard bits would be needed, i.e. for
+// exponent gaps of 0 or 1), then round to nearest, ties to even.  Zero and
+// subnormal operands, Inf, NaN and results that are subnormal or overflow
+// take the native add, so the result always equals __dadd_rn(a, b).
+__device__ __forceinline__ double dadd_int(double a, double b) {
+    unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    unsigned long long ma = ua & ~kSign, mb = ub & ~kSign;
+    if (ma < mb) {
+        const unsigned long long t = ua; ua = ub; ub = t;
+        const unsigned long long m = ma; ma = mb; mb = m;
+    }
+    const unsigned ea = (unsigned)(ma >> 52), eb = (unsigned)(mb >> 52);
+    if (eb == 0u || ea == 0x7FFu) return __dadd_rn(a, b);
+    const unsigned long long frac = 0xFFFFFFFFFFFFFull, one = 0x10000000000000ull;
+    const unsigned long long A = ((ma & frac) | one) << 10;
+    unsigned long long B = ((mb & frac) | one) << 10;
+    const unsigned d = ea - eb;
+    if (d >= 64u) B = 1ull;
+    else if (d) B = (B >> d) | ((B << (64u - d)) != 0ull ? 1ull : 0ull);
+    int e = (int)ea;
+    unsigned long long S;
+    if (((ua ^ ub) & kSign) == 0ull) {
+        S = A + B;
+        if (S >> 63) {
+            S = (S >> 1) | (S & 1ull);
+            e += 1;
+        }
+    } else {
+        S = A - B;
+        if (S == 0ull) return 0.0;  // x + (-x) = +0 under round to nearest
+        const int lz = __clzll((long long)S) - 1;
+        S <<= lz;
+        e -= lz;
+    }
+    unsigned long long M = S >> 10;
+    const unsigned long long R = S & 0x3FFull;
+    if (R > 0x200ull || (R == 0x200ull && (M & 1ull))) {
+        M += 1ull;
+        if (M >> 53) {
+            M >>= 1;
+            e += 1;
+        }
+    }
+    if (e <= 0 || e >= 0x7FF) return __dadd_rn(a, b);
+    return __longlong_as_double((long long)((ua & kSign) | ((unsigned long long)e << 52) | (M & frac)));
+}
+
+// a - b through dadd_int (negation is exact).
+__device__ __forceinline__ double dsub_int(double a, double b) { return dadd_int(a, flip(b)); }
+
 __device__ __forceinline__ bool gated(const Status* st, int gate) {
     return st->fault_gate < st->step * 8u + (unsigned)gate;
 }

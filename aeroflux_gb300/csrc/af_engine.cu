@@ -823,6 +823,15 @@ int af_selftest_div6(int device, int64_t n, uint64_t seed, int64_t* mismatches) 
     return AF_OK;
 }
 
+int af_selftest_dadd(int device, int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (!mismatches || n < 0 || device < 0) return AF_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return AF_ERR_CUDA;
+    unsigned long long bad = 0;
+    if (!af::selftest_dadd((unsigned long long)n, seed, &bad)) return AF_ERR_CUDA;
+    *mismatches = (int64_t)bad;
+    return AF_OK;
+}
+
 int af_device_fp64_rate(int device, double* fma_per_s) {
     if (!fma_per_s || device < 0) return AF_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return AF_ERR_CUDA;

@@ -14,6 +14,7 @@
 
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <cmath>
@@ -82,9 +83,23 @@ __device__ __forceinline__ double face_vel(const SweepArgs& a, int c, int x, int
     }
 }
 
-__device__ __forceinline__ double lerp(double a, double b, double t) {
-    // a*(1-t) + b*t, evaluated as the reference writes it
-    return dadd(dmul(a, dsub(1.0, t)), dmul(b, t));
+__device__ __forceinline__ double lerp(double a, double b, double t, double omt) {
+    // a*(1-t) + b*t as the reference writes it; omt = 1-t, the same bits the
+    // reference recomputes for every lerp
+    return dadd(dmul(a, omt), dmul(b, t));
+}
+
+// a*(1-t) + b*t for t = +0, with integer instructions: 1-t = 1 exactly, a*1
+// is a (NaN stays NaN), b*0 is a zero carrying b's sign when b is finite and
+// NaN otherwise, and a + (+-0) is a except that -0 + +0 = +0.
+__device__ __forceinline__ double lerp_t0(double a, double b) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    const bool b_nonfinite = (ub & 0x7FF0000000000000ull) == 0x7FF0000000000000ull;
+    const bool a_nan = (ua & ~kSign) > 0x7FF0000000000000ull;
+    if (b_nonfinite || a_nan) return __longlong_as_double(0x7FFFFFFFFFFFFFFFll);
+    if ((ua & ~kSign) == 0ull) return __longlong_as_double((long long)(ua & ub & kSign));
+    return a;
 }
 
 template <int AX>
@@ -146,13 +161,30 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     }
     const long long sy = d.sy, sz = d.sz;
     const long long b = (long long)i000;
-    const double c00 = lerp(sd[b], sd[b + 1], tx);
-    const double c10 = lerp(sd[b + sy], sd[b + sy + 1], tx);
-    const double c01 = lerp(sd[b + sz], sd[b + sz + 1], tx);
-    const double c11 = lerp(sd[b + sz + sy], sd[b + sz + sy + 1], tx);
-    const double c0 = lerp(c00, c10, ty);
-    const double c1 = lerp(c01, c11, ty);
-    const double adv = lerp(c0, c1, tz);
+    // Only the active axis has a nonzero weight; the lerps along the other
+    // two (weight exactly +0) run on the integer pipe with identical bits.
+    double adv;
+    if (AX == 0) {
+        const double omt = dsub(1.0, tx);
+        const double c00 = lerp(sd[b], sd[b + 1], tx, omt);
+        const double c10 = lerp(sd[b + sy], sd[b + sy + 1], tx, omt);
+        const double c01 = lerp(sd[b + sz], sd[b + sz + 1], tx, omt);
+        const double c11 = lerp(sd[b + sz + sy], sd[b + sz + sy + 1], tx, omt);
+        adv = lerp_t0(lerp_t0(c00, c10), lerp_t0(c01, c11));
+    } else if (AX == 1) {
+        const double omt = dsub(1.0, ty);
+        const double c00 = lerp_t0(sd[b], sd[b + 1]);
+        const double c10 = lerp_t0(sd[b + sy], sd[b + sy + 1]);
+        const double c01 = lerp_t0(sd[b + sz], sd[b + sz + 1]);
+        const double c11 = lerp_t0(sd[b + sz + sy], sd[b + sz + sy + 1]);
+        adv = lerp_t0(lerp(c00, c10, ty, omt), lerp(c01, c11, ty, omt));
+    } else {
+        const double c00 = lerp_t0(sd[b], sd[b + 1]);
+        const double c10 = lerp_t0(sd[b + sy], sd[b + sy + 1]);
+        const double c01 = lerp_t0(sd[b + sz], sd[b + sz + 1]);
+        const double c11 = lerp_t0(sd[b + sz + sy], sd[b + sz + sy + 1]);
+        adv = lerp(lerp_t0(c00, c10), lerp_t0(c01, c11), tz, dsub(1.0, tz));
+    }
 
     const long long i = (long long)x + (long long)y * sy + (long long)z * sz;
     double lap = 0.0;
@@ -188,6 +220,15 @@ __global__ void k_divergence_fp64(Geom g, const double* __restrict__ u, const do
 // cell's own pre-update value, so the sweep reads the centre instead and the
 // ghosts are materialised once, after the last sweep (k_pressure_bc).
 // ---------------------------------------------------------------------------
+// EMU selects which of the update's six binary64 add/subtracts run on the
+// integer pipe (bit k: operation k of the chain, the subtraction last); the
+// others issue on the FP64 pipe.  Every choice computes the same bits.
+template <int EMU>
+__device__ __forceinline__ double chain_add(int k, double a, double b) {
+    return ((EMU >> k) & 1) ? dadd_int(a, b) : dadd(a, b);
+}
+
+template <int EMU>
 __global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __restrict__ bb, int color, Status* st,
                             int gate) {
     if (gated(st, gate)) return;
@@ -207,8 +248,13 @@ __global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __rest
     const double yp = y < G + g.NY - 1 ? p[i + sy] : pc;
     const double zm = z > G ? p[i - sz] : pc;
     const double zp = z < G + g.NZ - 1 ? p[i + sz] : pc;
-    const double sum = dadd(dadd(dadd(dadd(dadd(xm, xp), ym), yp), zm), zp);
-    p[i] = div6_int(dsub(sum, bb[i]));
+    double sum = chain_add<EMU>(0, xm, xp);
+    sum = chain_add<EMU>(1, sum, ym);
+    sum = chain_add<EMU>(2, sum, yp);
+    sum = chain_add<EMU>(3, sum, zm);
+    sum = chain_add<EMU>(4, sum, zp);
+    const double r = ((EMU >> 5) & 1) ? dsub_int(sum, bb[i]) : dsub(sum, bb[i]);
+    p[i] = div6_int(r);
 }
 
 // applyPressureBC, project.go:139-163 (see pbc_cell).
@@ -412,6 +458,62 @@ __global__ void k_fp64_rate(double* out, double seed) {
 
 }  // namespace
 
+// dadd_int against __dadd_rn on pairs built to hit every path: random bit
+// patterns, close exponents (cancellation), exact ties, far exponents.
+__global__ void k_selftest_dadd(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        auto mix = [](unsigned long long z) {
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            return z ^ (z >> 31);
+        };
+        const unsigned long long r1 = mix(seed + (2 * i + 1) * 0x9E3779B97F4A7C15ull);
+        const unsigned long long r2 = mix(seed + (2 * i + 2) * 0x9E3779B97F4A7C15ull);
+        const unsigned long long ua = r1;
+        unsigned long long ub;
+        switch (i & 3) {
+        case 0: ub = r2; break;  // independent
+        case 1: {                // exponent within +-60 of a's, random sign
+            const long long ea = (long long)((ua >> 52) & 0x7FF);
+            long long eb = ea + (long long)(r2 % 121) - 60;
+            eb = eb < 0 ? 0 : (eb > 0x7FF ? 0x7FF : eb);
+            ub = (r2 & 0x8000000000000000ull) | ((unsigned long long)eb << 52) | ((r2 >> 11) & 0xFFFFFFFFFFFFFull);
+            break;
+        }
+        case 2: {                // same exponent and close significand: cancellation
+            ub = (r2 & 0x8000000000000000ull) | (ua & 0x7FF0000000000000ull) |
+                 ((ua + (r2 & 0xFFF) - 0x800) & 0xFFFFFFFFFFFFFull);
+            break;
+        }
+        default: {               // half an ulp of a (a tie) times a small power of two
+            const unsigned long long ea = (ua >> 52) & 0x7FF;
+            const unsigned long long sh = 53 + (r2 & 3);
+            const unsigned long long eb = ea > sh ? ea - sh : 0;
+            ub = (r2 & 0x8000000000000000ull) | (eb << 52) | (r2 & 0xFull);
+            break;
+        }
+        }
+        const double a = __longlong_as_double((long long)ua), b = __longlong_as_double((long long)ub);
+        const double ref = __dadd_rn(a, b), got = dadd_int(a, b), got2 = dsub_int(a, b), ref2 = __dsub_rn(a, b);
+        const bool ok = __double_as_longlong(got) == __double_as_longlong(ref) || (isnan(got) && isnan(ref));
+        const bool ok2 = __double_as_longlong(got2) == __double_as_longlong(ref2) || (isnan(got2) && isnan(ref2));
+        local += (ok ? 0 : 1) + (ok2 ? 0 : 1);
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+bool selftest_dadd(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
+    unsigned long long* bad = nullptr;
+    if (cudaMalloc(&bad, sizeof *bad) != cudaSuccess) return false;
+    cudaMemset(bad, 0, sizeof *bad);
+    k_selftest_dadd<<<152 * 8, 256>>>(n, seed, bad);
+    const bool ok = cudaMemcpy(mismatches, bad, sizeof *bad, cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(bad);
+    return ok && cudaGetLastError() == cudaSuccess;
+}
+
 bool selftest_div6(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
     unsigned long long* bad = nullptr;
     if (cudaMalloc(&bad, sizeof *bad) != cudaSuccess) return false;
@@ -489,10 +591,32 @@ void launch_divergence_fp64(const Geom& g, const Fields& f, double* b, double sc
     k_divergence_fp64<<<grid, block, 0, s>>>(g, f.u, f.v, f.w, f.p, f.div, b, scale, h2, zero_p ? 1 : 0, st, gate);
 }
 
+// Integer-pipe share of the red-black chain: AEROFLUX_RBGS_EMU picks the
+// mask.  Measured on GB300 at 256^3, every emulated add slows the update
+// (all six native: 41 ms per 200-pair projection; all six emulated: 146 ms),
+// so the default keeps the adds on the FP64 pipe; the exact /6 stays on the
+// integer pipe, where it wins over its three-operation FP64 sequence.
+static int rbgs_emu_mask() {
+    static int m = -1;
+    if (m < 0) {
+        const char* v = getenv("AEROFLUX_RBGS_EMU");
+        m = v ? atoi(v) : 0x00;
+    }
+    return m;
+}
+
 void launch_rbgs_fp64(const Geom& g, double* p, const double* b, int color, Status* st, int gate, cudaStream_t s) {
     dim3 block(32, 4);
     dim3 grid(cdiv((g.NX + 1) / 2, 32), cdiv(g.NY, 4), g.NZ);
-    k_rbgs_fp64<<<grid, block, 0, s>>>(g, p, b, color, st, gate);
+    switch (rbgs_emu_mask()) {
+    case 0x00: k_rbgs_fp64<0x00><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    case 0x01: k_rbgs_fp64<0x01><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    case 0x05: k_rbgs_fp64<0x05><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    case 0x15: k_rbgs_fp64<0x15><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    case 0x2A: k_rbgs_fp64<0x2A><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    case 0x35: k_rbgs_fp64<0x35><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    default: k_rbgs_fp64<0x3F><<<grid, block, 0, s>>>(g, p, b, color, st, gate); break;
+    }
 }
 
 void launch_pressure_bc_fp64(const Geom& g, double* p, Status* st, int gate, cudaStream_t s) {

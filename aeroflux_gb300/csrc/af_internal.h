@@ -94,6 +94,8 @@ cudaError_t seed_tg_fields(const Geom& g, double* u, double* v, double* w, doubl
 // Compares both exact /6 forms with IEEE division on n random bit patterns
 // (af_fp64.cu); false on a CUDA error.
 bool selftest_div6(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
+// Compares the integer-pipe binary64 add and subtract with the native ones.
+bool selftest_dadd(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
 
 // Binary64 FMA issue rate of the current device (independent chains, timed
 // with events); false on a CUDA error.

@@ -191,6 +191,11 @@ int af_last_step_profile(af_engine* e, af_step_profile* out);
  * results (NaN compared by NaN-ness). */
 int af_selftest_div6(int device, int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* Self-test of the integer-pipe binary64 add/subtract the red-black update
+ * uses against the native ones, on n pairs built from `seed` (random bit
+ * patterns, cancellations, exact ties, far exponents). */
+int af_selftest_dadd(int device, int64_t n, uint64_t seed, int64_t* mismatches);
+
 /* Measures the device's binary64 FMA issue rate (independent DFMA chains),
  * in FMA instructions per second, for the FP64 roofline. */
 int af_device_fp64_rate(int device, double* fma_per_s);

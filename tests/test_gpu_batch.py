@@ -70,6 +70,15 @@ def test_each_slot_is_bit_identical_to_its_grid_alone():
         assert divs[s] <= 1e-10
 
 
+def test_slot_with_odd_sweeps_in_an_even_batch_converges():
+    # The batch sweeps as often as its first slot; a slot whose own count
+    # has the other parity smooths in place instead of in fused pairs.
+    a = Config(**{**cfg(32, 32, 32).__dict__, "InnerSweeps": 2})
+    b_ = Config(**{**cfg(48, 24, 32).__dict__, "InnerSweeps": 3})
+    _, divs = batched([a, b_], 2)
+    assert max(divs) <= 1e-10
+
+
 def test_tuned_launch_shapes_do_not_change_results():
     a, _ = batched(SHAPES[:4], 2, tune=False)
     b, _ = batched(SHAPES[:4], 2, tune=True)

@@ -9,6 +9,7 @@ tolerance, orders below binary32 round-off), and whole Steps to ~1e-5
 relative (binary32 advection).  Every projection must reach the requested max|div|.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -48,6 +49,42 @@ def test_projection_reaches_tolerance(n):
     assert md <= 1e-10
     assert 1 <= passes <= e.Cfg.MaxRefine
     e.Close()
+
+
+@pytest.mark.parametrize("sweeps", [1, 3, 4])
+def test_projection_reaches_tolerance_with_any_sweep_count(sweeps):
+    # Odd counts smooth in place, even counts with fused red-black pairs.
+    e = seeded(mixed_cfg((48, 32, 96), InnerSweeps=sweeps))
+    e.project()
+    assert e.MaxDivergence() <= 1e-10
+    e.Close()
+
+
+def run_steps(n, steps, per_level, pairs):
+    env = {"AEROFLUX_MG_PER_LEVEL": "1" if per_level else "0", "AEROFLUX_MG_PAIRS": "1" if pairs else "0"}
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        e = seeded(mixed_cfg(n, DT=0.002))
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+    e.Step(steps)
+    out = np.concatenate([bits(e.download(k)) for k in ("U", "V", "W", "P")])
+    e.Close()
+    return out
+
+
+@pytest.mark.parametrize("n", [(32, 32, 32), (48, 32, 96), (64, 64, 64), (33, 17, 20)])
+def test_fused_pairs_and_tail_vcycle_equal_per_level_kernels(n):
+    # The fused red-black pair and the one-block tail V-cycle reorganise the
+    # per-level colour sweeps without changing any rounding: identical bits.
+    ref = run_steps(n, 2, True, False)
+    assert np.array_equal(run_steps(n, 2, False, False), ref)
+    assert np.array_equal(run_steps(n, 2, False, True), ref)
 
 
 def test_projection_matches_converged_fp64_oracle():
