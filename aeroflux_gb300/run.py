@@ -1,7 +1,7 @@
 """Runs one cubic workload through the engine and prints a JSON summary.
 
     python -m aeroflux_gb300.run --n 256 --steps 2 [--gsi 200] [--dt 0.001] [--nu 1e-5]
-                                 [--precision fp64|mixed] [--project N]
+                                 [--precision fp64|mixed] [--project N] [--inner-sweeps K] [--warmup W]
 
 --project N runs N projections (BC, divergence, red-black sweeps, gradient)
 instead of Steps.  The initial field is the seeded Taylor-Green vortex with
@@ -27,16 +27,20 @@ def main() -> None:
     ap.add_argument("--noise", type=float, default=0.01)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--project", type=int, default=0)
+    ap.add_argument("--inner-sweeps", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=0, help="untimed Steps (or projections) first")
     a = ap.parse_args()
     prec = AF_PRECISION_MIXED if a.precision == "mixed" else AF_PRECISION_FP64
     cfg = Config(NX=a.n, NY=a.n, NZ=a.n, H=1.0 / a.n, DT=a.dt, Viscosity=a.nu, Density=1.0,
-                 GaussSeidelIters=a.gsi, Precision=prec)
+                 GaussSeidelIters=a.gsi, Precision=prec, InnerSweeps=a.inner_sweeps)
     e = New(cfg)
     u, v, w = taylor_green(e.Cfg, 1.0, a.noise)
     e.upload("U", u)
     e.upload("V", v)
     e.upload("W", w)
     e.applyVelocityBC()
+    for _ in range(a.warmup):
+        e.project() if a.project else e.Step(1)
     t0 = time.perf_counter()
     if a.project:
         for _ in range(a.project):
@@ -48,6 +52,8 @@ def main() -> None:
     dt = time.perf_counter() - t0
     out = {"n": a.n, "precision": a.precision, "calls": n, "what": "project" if a.project else "step",
            "seconds": dt, "cell_steps_per_s": a.n ** 3 * n / dt, "max_divergence": e.MaxDivergence()}
+    if prec == AF_PRECISION_MIXED:
+        out["refinement_passes"] = e.LastProjectionStats()[0]
     print(json.dumps(out))
     e.Close()
 
