@@ -82,6 +82,7 @@ SIGNATURES = {
     "af_max_velocity": (C.c_int, [_E, C.POINTER(C.c_double)]),
     "af_cfl": (C.c_int, [_E, C.POINTER(C.c_double)]),
     "af_enable_sparse_solver": (C.c_int, [_E]),
+    "af_enable_multigrid_solver": (C.c_int, [_E, C.c_double]),
     "af_phase_sweep": (C.c_int, [_E, C.c_int, C.c_double]),
     "af_phase_divergence": (C.c_int, [_E]),
     "af_phase_red_black": (C.c_int, [_E]),

@@ -381,9 +381,14 @@ __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaG
         c.maxr_bits = 0;
         if (c.stopped) continue;
         const double div = I.res_scale * r;
+        // A pass that removes less than a tenth of max|r| has reached the
+        // binary64 round-off floor of the residual (|B| * 2^-53 and up):
+        // stop there rather than spin to the pass cap.
+        const bool stalled = count_pass && div > 0.9 * c.last_div;
         c.last_div = div;
         if (count_pass) c.passes += 1;
-        const bool more = !gated(&st[s], gate) && div > I.thresh && !isinf(div) && c.passes < I.max_refine;
+        const bool more =
+            !gated(&st[s], gate) && div > I.thresh && !isinf(div) && !stalled && c.passes < I.max_refine;
         if (!more) c.stopped = 1;
         any |= more ? 1 : 0;
     }
@@ -1508,10 +1513,9 @@ cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err) {
     return cudaSuccess;
 }
 
-cudaError_t batch_project(Batch* b, std::string* err) {
+cudaError_t batch_prepare_capture(Batch* b) {
     cudaError_t rc;
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
-    if ((rc = reset_status(b)) != cudaSuccess) return rc;
     if (max_levels(b) > b->graph_levels && b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -1521,8 +1525,34 @@ cudaError_t batch_project(Batch* b, std::string* err) {
     b->graph_pair |= smooth_levels(b, true);
     b->graph_single |= smooth_levels(b, false);
     b->tail_smem = std::max(b->tail_smem, tail_smem_bytes(b));
-    cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem);
+    if ((rc = cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem)) !=
+        cudaSuccess)
+        return rc;
     size_grids(b);
+    return cudaSuccess;
+}
+
+int64_t batch_enqueue_project(Batch* b, int parity, int gate, cudaStream_t s) {
+    const int64_t before = b->launches;
+    const bool prof = b->profiling;
+    b->profiling = false;
+    enq_project(b, parity, gate, s);
+    b->profiling = prof;
+    return b->launches - before;
+}
+
+cudaError_t batch_capture_error(Batch* b) {
+    const cudaError_t rc = b->capture_err;
+    b->capture_err = cudaSuccess;
+    return rc;
+}
+
+Status* batch_status(Batch* b, int slot) { return b->d_st + slot; }
+
+cudaError_t batch_project(Batch* b, std::string* err) {
+    cudaError_t rc;
+    if ((rc = batch_prepare_capture(b)) != cudaSuccess) return rc;
+    if ((rc = reset_status(b)) != cudaSuccess) return rc;
     cudaGraphExec_t g = nullptr;
     const bool prof = b->profiling;
     b->profiling = false;

@@ -42,6 +42,15 @@ cudaStream_t batch_stream(Batch* b);
 cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err);
 // One projection (project.go:12-34) of every active slot, as a graph.
 cudaError_t batch_project(Batch* b, std::string* err);
+// A projection inside a caller's own graph (the FP64 engine's multigrid
+// option): prepare before the caller begins capturing; enqueue on the
+// caller's capturing stream with the caller's field parity and fault gate
+// (returns the kernel launches it added); after capture, check the error the
+// enqueue may have recorded.  Faults go to batch_status(b, slot).
+cudaError_t batch_prepare_capture(Batch* b);
+int64_t batch_enqueue_project(Batch* b, int parity, int gate, cudaStream_t s);
+cudaError_t batch_capture_error(Batch* b);
+Status* batch_status(Batch* b, int slot);
 // applyVelocityBC of every active slot.
 cudaError_t batch_velocity_bc(Batch* b);
 // One sweep (dispatch + commit) of every active slot.

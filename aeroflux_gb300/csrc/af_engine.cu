@@ -20,6 +20,7 @@
 #include <sched.h>
 
 #include <algorithm>
+#include <cmath>
 #include <new>
 #include <string>
 #include <thread>
@@ -201,6 +202,11 @@ struct af_engine {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     af::Batch* batch = nullptr;  // MIXED form: a batch of one over this arena
+    // FP64 form with the multigrid projection option: a batch of one over
+    // this arena supplies the projection; `st` then points at its status
+    // word and `own_st` keeps the engine's own for release.
+    af::Batch* mg = nullptr;
+    Status* own_st = nullptr;
     // Profiling: event nodes at the step's ends, around each sweep and around
     // each projection's red-black loop.
     bool profiling = false;
@@ -318,7 +324,17 @@ void enqueue_project_fp64(af_engine* e, const Fields& f, int gate) {
     af::launch_velocity_bc(g, f.u, f.v, f.w, e->st, gate, s);
 }
 
-void enqueue_project(af_engine* e, const Fields& f, int gate) { enqueue_project_fp64(e, f, gate); }
+// `parity` is the U/V/W slot parity at this point of the step (the
+// multigrid projection addresses fields through the batch's slot table).
+void enqueue_project(af_engine* e, const Fields& f, int gate, int parity) {
+    if (!e->mg) {
+        enqueue_project_fp64(e, f, gate);
+        return;
+    }
+    rec(e, kEvRb + (gate == 3 ? 0 : 2));
+    e->launches_per_step += af::batch_enqueue_project(e->mg, parity, gate, e->stream);
+    rec(e, kEvRb + (gate == 3 ? 1 : 3));
+}
 
 void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {
     const Geom& g = e->geom;
@@ -340,9 +356,9 @@ void enqueue_step(af_engine* e) {
     rec(e, kEvStart);
     const double half = e->cfg.dt * 0.5;  // aeroflux.go:353
     for (int k = 0; k < 3; ++k) enqueue_sweep(e, f, kFwd[k], half, k);
-    enqueue_project(e, f, 3);
+    enqueue_project(e, f, 3, e->parity ^ 1);
     for (int k = 0; k < 3; ++k) enqueue_sweep(e, f, kRev[k], half, 3 + k);
-    enqueue_project(e, f, 6);
+    enqueue_project(e, f, 6, e->parity);
     af::launch_step_tick(e->st, e->stream);
     rec(e, kEvEnd);
 }
@@ -361,7 +377,27 @@ int capture(af_engine* e, F body, cudaGraphExec_t* out) {
     return AF_OK;
 }
 
-int build_graph(af_engine* e) { return capture(e, [&] { enqueue_step(e); }, &e->graph[e->parity]); }
+// Captures `body`; with the multigrid option the batch's tables are
+// prepared first and an error its enqueue recorded fails the capture.
+template <class F>
+int capture_step(af_engine* e, F body, cudaGraphExec_t* out) {
+    if (e->mg) {
+        const cudaError_t rc = af::batch_prepare_capture(e->mg);
+        if (rc != cudaSuccess) return cuda_fail(e, rc, "preparing the multigrid projection");
+    }
+    if (int rc = capture(e, body, out)) return rc;
+    if (e->mg) {
+        const cudaError_t rc = af::batch_capture_error(e->mg);
+        if (rc != cudaSuccess) {
+            cudaGraphExecDestroy(*out);
+            *out = nullptr;
+            return cuda_fail(e, rc, "capturing the multigrid projection");
+        }
+    }
+    return AF_OK;
+}
+
+int build_graph(af_engine* e) { return capture_step(e, [&] { enqueue_step(e); }, &e->graph[e->parity]); }
 
 std::string fault_message(const af_engine* e, unsigned gate, unsigned long long key) {
     return af::fault_message_for(e->geom, gate, key);
@@ -376,8 +412,14 @@ int release(af_engine* e) {
     drop_graphs(e);
     for (auto& ev : e->ev)
         if (ev) { cudaEventDestroy(ev); ev = nullptr; }
-    if (e->batch) { af::batch_destroy(e->batch); e->batch = nullptr; }
     if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->batch) { af::batch_destroy(e->batch); e->batch = nullptr; }
+    if (e->mg) {
+        af::batch_destroy(e->mg);
+        e->mg = nullptr;
+        e->st = e->own_st;
+        e->own_st = nullptr;
+    }
     cudaFree(e->arena);
     cudaFree(e->b);
     cudaFree(e->st);
@@ -614,7 +656,18 @@ int af_project(af_engine* e) {
         return batch_check(e, rc, err);
     }
     if (int rc = reset_status(e)) return rc;
-    enqueue_project(e, e->fields(), 0);
+    if (e->mg) {
+        // The multigrid projection's refinement loop is a conditional graph
+        // node, so even a single projection runs as a captured graph.
+        cudaGraphExec_t g = nullptr;
+        if (int rc = capture_step(e, [&] { enqueue_project(e, e->fields(), 0, e->parity); }, &g)) return rc;
+        const cudaError_t lr = cudaGraphLaunch(g, e->stream);
+        cudaStreamSynchronize(e->stream);
+        cudaGraphExecDestroy(g);
+        AF_CUDA(e, lr);
+        return sync_and_check(e);
+    }
+    enqueue_project(e, e->fields(), 0, e->parity);
     AF_CUDA(e, cudaGetLastError());
     return sync_and_check(e);
 }
@@ -755,9 +808,47 @@ int af_enable_sparse_solver(af_engine* e) {
     return AF_ERR_UNSUPPORTED;
 }
 
+int af_enable_multigrid_solver(af_engine* e, double div_tol) {
+    if (int rc = check_open(e)) return rc;
+    if (e->batch) {
+        e->err = "aeroflux: the mixed-precision form already projects with multigrid";
+        return AF_ERR_UNSUPPORTED;
+    }
+    if (e->mg) return AF_OK;  // EnableSparseSolver is idempotent (sparse_darwin.go:26-29)
+    if (div_tol == 0.0) div_tol = 1e-12;
+    if (!(div_tol > 0.0) || !std::isfinite(div_tol)) {
+        e->err = sfmt("aeroflux: multigrid divergence tolerance must be positive and finite, got %g", div_tol);
+        return AF_ERR_ARG;
+    }
+    AF_CUDA(e, cudaStreamSynchronize(e->stream));
+    af_config mc = e->cfg;
+    mc.precision = AF_PRECISION_MIXED;
+    mc.div_tol = div_tol;
+    if (mc.inner_sweeps < 1) mc.inner_sweeps = 2;
+    if (mc.max_refine < 1) mc.max_refine = 30;
+    std::string merr;
+    af::Batch* b = af::batch_create(1, 0, &merr);
+    if (!b || af::batch_assign(b, mc, e->arena, &merr) != 0) {
+        if (b) af::batch_destroy(b);
+        e->err = merr.empty() ? "aeroflux: multigrid solver setup failed" : merr;
+        return AF_ERR_NOMEM;
+    }
+    e->mg = b;
+    e->own_st = e->st;
+    e->st = af::batch_status(b, 0);
+    e->cfg.div_tol = div_tol;
+    drop_graphs(e);  // recaptured with the multigrid projection and the new status word
+    return reset_status(e);
+}
+
 int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div) {
     if (int rc = check_open(e)) return rc;
     if (!passes || !max_div) return AF_ERR_ARG;
+    if (e->mg) {
+        AF_CUDA(e, cudaStreamSynchronize(e->stream));
+        af::batch_slot_projection(e->mg, 0, passes, max_div);
+        return AF_OK;
+    }
     if (!e->batch) {
         *passes = 0;
         return af_max_divergence(e, max_div);

@@ -233,6 +233,12 @@ class Engine:
     def EnableSparseSolver(self) -> None:
         self._check(L.lib().af_enable_sparse_solver(self._h))
 
+    def EnableMultigridSolver(self, div_tol: float = 0.0) -> None:
+        """The GPU analogue of EnableSparseSolver (sparse_darwin.go:26-132):
+        projections solve to max|div| <= div_tol (0: 1e-12) by binary64
+        refinement around binary32 multigrid; the sweeps stay bit-exact."""
+        self._check(L.lib().af_enable_multigrid_solver(self._h, div_tol))
+
     def Close(self) -> None:
         """(*Engine).Close, aeroflux.go:419-439; idempotent."""
         if self._h:

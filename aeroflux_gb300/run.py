@@ -2,6 +2,7 @@
 
     python -m aeroflux_gb300.run --n 256 --steps 2 [--gsi 200] [--dt 0.001] [--nu 1e-5]
                                  [--precision fp64|mixed] [--project N] [--inner-sweeps K] [--warmup W]
+                                 [--multigrid TOL]
 
 --project N runs N projections (BC, divergence, red-black sweeps, gradient)
 instead of Steps.  The initial field is the seeded Taylor-Green vortex with
@@ -29,6 +30,8 @@ def main() -> None:
     ap.add_argument("--project", type=int, default=0)
     ap.add_argument("--inner-sweeps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=0, help="untimed Steps (or projections) first")
+    ap.add_argument("--multigrid", type=float, default=None, metavar="TOL",
+                    help="FP64 form with the multigrid projection to max|div| <= TOL (0: 1e-12)")
     a = ap.parse_args()
     prec = AF_PRECISION_MIXED if a.precision == "mixed" else AF_PRECISION_FP64
     cfg = Config(NX=a.n, NY=a.n, NZ=a.n, H=1.0 / a.n, DT=a.dt, Viscosity=a.nu, Density=1.0,
@@ -39,6 +42,8 @@ def main() -> None:
     e.upload("V", v)
     e.upload("W", w)
     e.applyVelocityBC()
+    if a.multigrid is not None:
+        e.EnableMultigridSolver(a.multigrid)
     for _ in range(a.warmup):
         e.project() if a.project else e.Step(1)
     t0 = time.perf_counter()
@@ -52,7 +57,7 @@ def main() -> None:
     dt = time.perf_counter() - t0
     out = {"n": a.n, "precision": a.precision, "calls": n, "what": "project" if a.project else "step",
            "seconds": dt, "cell_steps_per_s": a.n ** 3 * n / dt, "max_divergence": e.MaxDivergence()}
-    if prec == AF_PRECISION_MIXED:
+    if prec == AF_PRECISION_MIXED or a.multigrid is not None:
         out["refinement_passes"] = e.LastProjectionStats()[0]
     print(json.dumps(out))
     e.Close()

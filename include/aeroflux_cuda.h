@@ -154,6 +154,21 @@ int af_cfl(af_engine* e, double* out);
  * AF_ERR_UNSUPPORTED with the reference's fallback message. */
 int af_enable_sparse_solver(af_engine* e);
 
+/* The GPU analogue of EnableSparseSolver on Darwin (sparse_darwin.go:26-132,
+ * used by project.go:19-27): from the next projection on, the FP64 engine
+ * solves the pressure Poisson problem to max|div| <= div_tol (0 selects
+ * 1e-12, "exact projection") by binary64 iterative refinement around
+ * binary32 multigrid V-cycles instead of GaussSeidelIters red-black sweeps;
+ * where the binary64 residual's round-off floor (about |h^2*Div| * 2^-53,
+ * scaled by dt/(rho h^2)) lies above div_tol, refinement stops at the floor
+ * (a pass that removes less than a tenth of max|r|).
+ * The sweeps stay bit-identical to the reference; P is the refined solution
+ * (its additive constant differs from the pinned-cell Cholesky solution,
+ * which the gradient does not see).  Idempotent like EnableSparseSolver;
+ * AF_ERR_UNSUPPORTED for the mixed-precision form (which already projects
+ * this way).  af_last_projection_stats reports its passes. */
+int af_enable_multigrid_solver(af_engine* e, double div_tol);
+
 /* Phase hooks, one reference phase each, for stage-level parity tests:
  * dispatch(sweepFn)+commitVelocity for one axis (0=x,1=y,2=z) at dt
  * (stencil.go:21-25,230-235), computeDivergence (project.go:42-62),
