@@ -26,6 +26,9 @@ AF_ERR_NOMEM = -7
 AF_PRECISION_FP64 = 0
 AF_PRECISION_MIXED = 1
 
+AF_ADVECTION_SEMI_LAGRANGIAN = 0
+AF_ADVECTION_MACCORMACK = 1
+
 
 class AfConfig(C.Structure):
     _fields_ = [
@@ -83,6 +86,7 @@ SIGNATURES = {
     "af_cfl": (C.c_int, [_E, C.POINTER(C.c_double)]),
     "af_enable_sparse_solver": (C.c_int, [_E]),
     "af_enable_multigrid_solver": (C.c_int, [_E, C.c_double]),
+    "af_set_advection": (C.c_int, [_E, C.c_int]),
     "af_phase_sweep": (C.c_int, [_E, C.c_int, C.c_double]),
     "af_phase_divergence": (C.c_int, [_E]),
     "af_phase_red_black": (C.c_int, [_E]),

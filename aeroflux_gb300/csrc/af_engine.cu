@@ -207,6 +207,10 @@ struct af_engine {
     // word and `own_st` keeps the engine's own for release.
     af::Batch* mg = nullptr;
     Status* own_st = nullptr;
+    // Advection scheme (af_advection); MacCormack keeps its forward step in
+    // three face fields shaped like U, V, W.
+    int advection = AF_ADVECTION_SEMI_LAGRANGIAN;
+    char* mc_scratch = nullptr;
     // Profiling: event nodes at the step's ends, around each sweep and around
     // each projection's red-black loop.
     bool profiling = false;
@@ -336,15 +340,29 @@ void enqueue_project(af_engine* e, const Fields& f, int gate, int parity) {
     rec(e, kEvRb + (gate == 3 ? 1 : 3));
 }
 
-void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {
+// The sweep kernels of one axis: the reference's semi-Lagrangian sweep, or
+// its MacCormack form.  Returns the launches.
+int launch_advect(af_engine* e, const Fields& f, int axis, double dt, int phase) {
     const Geom& g = e->geom;
     const double invH = 1.0 / e->cfg.h;
     const double lam = e->cfg.viscosity * dt * invH * invH;  // stencil.go:73
-    af::launch_velocity_bc(g, f.u, f.v, f.w, e->st, phase, e->stream);
-    rec(e, kEvSweep + 2 * phase);
+    if (e->advection == AF_ADVECTION_MACCORMACK) {
+        Fields fwd = f;
+        fwd.t0 = (double*)e->mc_scratch;
+        fwd.t1 = fwd.t0 + ((g.u.count + 15) & ~15ll);
+        fwd.t2 = fwd.t1 + ((g.v.count + 15) & ~15ll);
+        af::launch_maccormack_fp64(g, axis, f, fwd, dt, invH, lam, e->st, phase, e->stream);
+        return 2;
+    }
     af::launch_sweep_fp64(g, axis, f, dt, invH, lam, e->st, phase, e->stream);
+    return 1;
+}
+
+void enqueue_sweep(af_engine* e, Fields& f, int axis, double dt, int phase) {
+    af::launch_velocity_bc(e->geom, f.u, f.v, f.w, e->st, phase, e->stream);
+    rec(e, kEvSweep + 2 * phase);
+    e->launches_per_step += 1 + launch_advect(e, f, axis, dt, phase);
     rec(e, kEvSweep + 2 * phase + 1);
-    e->launches_per_step += 2;
     swap_fields(f);  // commitVelocity, stencil.go:230-235
 }
 
@@ -420,6 +438,8 @@ int release(af_engine* e) {
         e->st = e->own_st;
         e->own_st = nullptr;
     }
+    cudaFree(e->mc_scratch);
+    e->mc_scratch = nullptr;
     cudaFree(e->arena);
     cudaFree(e->b);
     cudaFree(e->st);
@@ -680,10 +700,7 @@ int af_phase_sweep(af_engine* e, int axis, double dt) {
     }
     if (e->batch) return batch_check(e, af::batch_sweep(e->batch, axis, dt), "");
     if (int rc = reset_status(e)) return rc;
-    Fields f = e->fields();
-    const double invH = 1.0 / e->cfg.h;
-    const double lam = e->cfg.viscosity * dt * invH * invH;
-    af::launch_sweep_fp64(e->geom, axis, f, dt, invH, lam, e->st, 0, e->stream);
+    launch_advect(e, e->fields(), axis, dt, 0);
     AF_CUDA(e, cudaGetLastError());
     Status s;
     AF_CUDA(e, cudaMemcpyAsync(&s, e->st, sizeof s, cudaMemcpyDeviceToHost, e->stream));
@@ -839,6 +856,35 @@ int af_enable_multigrid_solver(af_engine* e, double div_tol) {
     e->cfg.div_tol = div_tol;
     drop_graphs(e);  // recaptured with the multigrid projection and the new status word
     return reset_status(e);
+}
+
+int af_set_advection(af_engine* e, int scheme) {
+    if (int rc = check_open(e)) return rc;
+    if (scheme != AF_ADVECTION_SEMI_LAGRANGIAN && scheme != AF_ADVECTION_MACCORMACK) {
+        e->err = sfmt("aeroflux: unknown advection scheme %d", scheme);
+        return AF_ERR_ARG;
+    }
+    if (e->batch) {
+        if (scheme == AF_ADVECTION_SEMI_LAGRANGIAN) return AF_OK;
+        e->err = "aeroflux: MacCormack advection is available in the FP64 form only";
+        return AF_ERR_UNSUPPORTED;
+    }
+    if (scheme == e->advection) return AF_OK;
+    AF_CUDA(e, cudaStreamSynchronize(e->stream));
+    if (scheme == AF_ADVECTION_MACCORMACK && !e->mc_scratch) {
+        const Geom& g = e->geom;
+        const size_t n = (size_t)((g.u.count + 15) & ~15ll) + (size_t)((g.v.count + 15) & ~15ll) + (size_t)g.w.count;
+        const cudaError_t rc = cudaMalloc(&e->mc_scratch, n * sizeof(double));
+        if (rc != cudaSuccess) {
+            cudaGetLastError();
+            e->mc_scratch = nullptr;
+            e->err = sfmt("aeroflux: MacCormack scratch of %zu bytes: %s", n * sizeof(double), cudaGetErrorString(rc));
+            return AF_ERR_NOMEM;
+        }
+    }
+    e->advection = scheme;
+    drop_graphs(e);
+    return AF_OK;
 }
 
 int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div) {

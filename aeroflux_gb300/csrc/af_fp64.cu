@@ -196,6 +196,71 @@ __global__ void k_sweep_fp64(SweepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// MacCormack correction of one axis sweep (Selle, Fedkiw, Kim, Liu, Rossignac,
+// "An Unconditionally Stable MacCormack Method", J. Sci. Comput. 2008), the
+// higher-order advection the reference lists as its missing remedy for
+// semi-Lagrangian dissipation (README "Known limitations").  The forward
+// step is the reference sweep itself run with lam = 0 into `fwd` (phi^ =
+// semi-Lagrangian advection of the component, faults and all); this kernel
+// traces the same face velocity forward (x + dt*v*invH) through phi^ to get
+// phi~, forms phi^ + (phi - phi~)/2, falls back to phi^ where that leaves the
+// range of the two source values the forward step interpolated (the limiter
+// that keeps the scheme unconditionally stable), and adds the reference's
+// directional diffusion of phi.  Along the sweep axis only: the tangential
+// weights are zero, as in the forward step.  Taps of phi^ outside the faces
+// the sweep writes read phi (the boundary-conditioned field) instead.
+template <int AX>
+__global__ void k_maccormack_fp64(SweepArgs a, const double* fu, const double* fv, const double* fw) {
+    if (gated(a.st, a.phase)) return;
+    const int zr = a.NZ + 1;
+    const int c = blockIdx.z / zr;
+    const int z = a.G + (int)(blockIdx.z % zr);
+    const int x = a.G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = a.G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int x1 = a.G + a.NX + (c == 0), y1 = a.G + a.NY + (c == 1), z1 = a.G + a.NZ + (c == 2);
+    if (x >= x1 || y >= y1 || z >= z1) return;
+
+    const Dims& d = c == 0 ? a.du : (c == 1 ? a.dv : a.dw);
+    const double* sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
+    const double* fd = c == 0 ? fu : (c == 1 ? fv : fw);
+    double* dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
+    const long long sy = d.sy, sz = d.sz;
+    const long long step = AX == 0 ? 1 : (AX == 1 ? sy : sz);
+    const long long i = (long long)x + (long long)y * sy + (long long)z * sz;
+    const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+    const int lo = a.G, hi = AX == 0 ? x1 - 1 : (AX == 1 ? y1 - 1 : z1 - 1);  // written faces on the axis
+    const double fwd = fd[i];
+
+    double lap = 0.0;
+    if (a.lam != 0) lap = dmul(a.lam, dadd(dsub(sd[i - step], dmul(2.0, sd[i])), sd[i + step]));
+
+    const double shift = dmul(dmul(a.dt, face_vel<AX>(a, c, x, y, z)), a.invH);
+    const double maxA = (double)(na - 1);
+    // Forward foot (the one the forward step sampled) and backward foot.
+    double pf = dsub((double)ca, shift), pb = dadd((double)ca, shift);
+    if (isnan(pf) || isnan(pb)) {  // the forward step has dealt with it
+        dd[i] = dadd(fwd, lap);
+        return;
+    }
+    pf = fmin(fmax(pf, 0.0), maxA);
+    pb = fmin(fmax(pb, 0.0), maxA);
+    long long f0 = (long long)pf, b0 = (long long)pb;
+    if (f0 >= na - 1) f0 = na - 2;
+    if (b0 >= na - 1) b0 = na - 2;
+    const long long base = i - (long long)ca * step;  // the face's row at axis coordinate 0
+    const double s0 = sd[base + f0 * step], s1 = sd[base + (f0 + 1) * step];
+    const double mn = fmin(s0, s1), mx = fmax(s0, s1);
+    auto phi_hat = [&](long long k) { return (k >= lo && k <= hi) ? fd[base + k * step] : sd[base + k * step]; };
+    const double tb = dsub(pb, (double)b0);
+    const double back = dadd(dmul(phi_hat(b0), dsub(1.0, tb)), dmul(phi_hat(b0 + 1), tb));
+    double out = dadd(fwd, dmul(0.5, dsub(sd[i], back)));
+    if (!(out >= mn && out <= mx)) out = fwd;
+    dd[i] = dadd(out, lap);
+}
+
+
+// ---------------------------------------------------------------------------
 // solvePressureRedBlack's zeroing (project.go:81-83) fused with
 // computeDivergence (project.go:42-62).  Also stores B = h2*Div, the product
 // every red-black update recomputes (project.go:126), so the sweeps read it
@@ -582,6 +647,24 @@ void launch_sweep_fp64(const Geom& g, int axis, const Fields& f, double dt, doub
     if (axis == 0) k_sweep_fp64<0><<<grid, block, 0, s>>>(a);
     else if (axis == 1) k_sweep_fp64<1><<<grid, block, 0, s>>>(a);
     else k_sweep_fp64<2><<<grid, block, 0, s>>>(a);
+}
+
+void launch_maccormack_fp64(const Geom& g, int axis, const Fields& f, const Fields& fwd, double dt, double invH,
+                            double lam, Status* st, int phase, cudaStream_t s) {
+    // Forward step: the reference sweep without diffusion, into fwd.t0..t2.
+    launch_sweep_fp64(g, axis, fwd, dt, invH, 0.0, st, phase, s);
+    SweepArgs a;
+    a.u = f.u; a.v = f.v; a.w = f.w;
+    a.tu = f.t0; a.tv = f.t1; a.tw = f.t2;
+    a.du = g.u; a.dv = g.v; a.dw = g.w;
+    a.NX = g.NX; a.NY = g.NY; a.NZ = g.NZ; a.G = g.G;
+    a.dt = dt; a.invH = invH; a.lam = lam;
+    a.st = st; a.phase = phase;
+    dim3 block(64, 4);
+    dim3 grid(cdiv(g.NX + 1, 64), cdiv(g.NY + 1, 4), 3 * (g.NZ + 1));
+    if (axis == 0) k_maccormack_fp64<0><<<grid, block, 0, s>>>(a, fwd.t0, fwd.t1, fwd.t2);
+    else if (axis == 1) k_maccormack_fp64<1><<<grid, block, 0, s>>>(a, fwd.t0, fwd.t1, fwd.t2);
+    else k_maccormack_fp64<2><<<grid, block, 0, s>>>(a, fwd.t0, fwd.t1, fwd.t2);
 }
 
 void launch_divergence_fp64(const Geom& g, const Fields& f, double* b, double scale, double h2, bool zero_p,

@@ -62,6 +62,11 @@ struct Fields {
 void launch_velocity_bc(const Geom& g, double* u, double* v, double* w, Status* st, int gate, cudaStream_t s);
 void launch_sweep_fp64(const Geom& g, int axis, const Fields& f, double dt, double invH, double lam,
                        Status* st, int phase, cudaStream_t s);
+// MacCormack form of the same sweep: forward semi-Lagrangian step into
+// fwd.t0..t2 (fwd.u/v/w = f.u/v/w), then the limited correction plus the
+// directional diffusion into f.t0..t2.  Two launches.
+void launch_maccormack_fp64(const Geom& g, int axis, const Fields& f, const Fields& fwd, double dt, double invH,
+                            double lam, Status* st, int phase, cudaStream_t s);
 // zero_p also zeroes all of P, as solvePressureRedBlack does first (project.go:81-83).
 void launch_divergence_fp64(const Geom& g, const Fields& f, double* b, double scale, double h2, bool zero_p,
                             Status* st, int gate, cudaStream_t s);

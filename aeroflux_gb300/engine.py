@@ -239,6 +239,11 @@ class Engine:
         refinement around binary32 multigrid; the sweeps stay bit-exact."""
         self._check(L.lib().af_enable_multigrid_solver(self._h, div_tol))
 
+    def SetAdvection(self, scheme: int) -> None:
+        """AF_ADVECTION_SEMI_LAGRANGIAN (the reference's, bit-exact) or
+        AF_ADVECTION_MACCORMACK (limited MacCormack, FP64 form only)."""
+        self._check(L.lib().af_set_advection(self._h, scheme))
+
     def Close(self) -> None:
         """(*Engine).Close, aeroflux.go:419-439; idempotent."""
         if self._h:

@@ -2,7 +2,7 @@
 
     python -m aeroflux_gb300.run --n 256 --steps 2 [--gsi 200] [--dt 0.001] [--nu 1e-5]
                                  [--precision fp64|mixed] [--project N] [--inner-sweeps K] [--warmup W]
-                                 [--multigrid TOL]
+                                 [--multigrid TOL] [--maccormack]
 
 --project N runs N projections (BC, divergence, red-black sweeps, gradient)
 instead of Steps.  The initial field is the seeded Taylor-Green vortex with
@@ -14,7 +14,7 @@ import argparse
 import json
 import time
 
-from . import AF_PRECISION_FP64, AF_PRECISION_MIXED, Config, New
+from . import AF_ADVECTION_MACCORMACK, AF_PRECISION_FP64, AF_PRECISION_MIXED, Config, New
 from .workloads import taylor_green
 
 
@@ -30,6 +30,7 @@ def main() -> None:
     ap.add_argument("--project", type=int, default=0)
     ap.add_argument("--inner-sweeps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=0, help="untimed Steps (or projections) first")
+    ap.add_argument("--maccormack", action="store_true", help="FP64 form with MacCormack advection")
     ap.add_argument("--multigrid", type=float, default=None, metavar="TOL",
                     help="FP64 form with the multigrid projection to max|div| <= TOL (0: 1e-12)")
     a = ap.parse_args()
@@ -44,6 +45,8 @@ def main() -> None:
     e.applyVelocityBC()
     if a.multigrid is not None:
         e.EnableMultigridSolver(a.multigrid)
+    if a.maccormack:
+        e.SetAdvection(AF_ADVECTION_MACCORMACK)
     for _ in range(a.warmup):
         e.project() if a.project else e.Step(1)
     t0 = time.perf_counter()

@@ -169,6 +169,21 @@ int af_enable_sparse_solver(af_engine* e);
  * this way).  af_last_projection_stats reports its passes. */
 int af_enable_multigrid_solver(af_engine* e, double div_tol);
 
+/* Advection scheme of the FP64 form's sweeps.  SEMI_LAGRANGIAN is the
+ * reference's (stencil.go:44-119), bit-exact.  MACCORMACK is the higher-order
+ * form the reference names as the remedy for its numerical dissipation
+ * (README "Known limitations"): per axis sweep the reference's
+ * semi-Lagrangian step, a backward trace through its result, the
+ * error-compensating correction limited to the range of the sampled source
+ * values (Selle et al. 2008), then the reference's directional diffusion.
+ * Two launches per sweep and three extra face fields of device memory.
+ * AF_ERR_UNSUPPORTED for MACCORMACK in the mixed-precision form. */
+typedef enum af_advection {
+    AF_ADVECTION_SEMI_LAGRANGIAN = 0,
+    AF_ADVECTION_MACCORMACK = 1
+} af_advection;
+int af_set_advection(af_engine* e, int scheme);
+
 /* Phase hooks, one reference phase each, for stage-level parity tests:
  * dispatch(sweepFn)+commitVelocity for one axis (0=x,1=y,2=z) at dt
  * (stencil.go:21-25,230-235), computeDivergence (project.go:42-62),
