@@ -97,13 +97,14 @@ struct InstDev {
     FastDiv fpx, fpy;        // padded P extents
     FastDiv ffx, ffy, ffz;   // NX+1, NY+1, NZ+1 (the face box)
     FastDiv fnx, fny;        // NX, NY
+    float* sh[3];            // binary32 shadow of the current U, V, W (the sweeps' taps)
     Lvl lev[kMaxLev];
 };
 
 // Stage ids.  Level stages take kMaxLev consecutive ids.
 enum {
-    S_BC = 0, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD, S_COARSE,
-    S_SMOOTH = 7,
+    S_BC = 0, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD, S_COARSE, S_SHADOW,
+    S_SMOOTH = 8,
     S_RESTRICT = S_SMOOTH + kMaxLev,
     S_PROLONG = S_RESTRICT + kMaxLev,
     S_BIGCOARSE = S_PROLONG + kMaxLev,
@@ -250,25 +251,51 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
     END_TILES
 }
 
+// binary32 shadow of the current U, V, W (every element, ghosts included),
+// converted once per sweep instead of once per tap.
+__global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
+    FOR_TILES(tab)
+    const InstDev& I = inst[s];
+    const long long nu = I.g.u.count, nv = I.g.v.count, n = nu + nv + I.g.w.count;
+    const double* u = cur(I, 1, parity);
+    const double* v = cur(I, 2, parity);
+    const double* w = cur(I, 3, parity);
+    FOR_ELEMS(tab)
+    if (el >= n) break;
+    if (el < nu) I.sh[0][el] = f64_to_f32(u[el]);
+    else if (el < nu + nv) I.sh[1][el - nu] = f64_to_f32(v[el - nu]);
+    else I.sh[2][el - nu - nv] = f64_to_f32(w[el - nu - nv]);
+    END_ELEMS
+    END_TILES
+}
+
+// One axis sweep of every face.  A warp owns one (component, y, z) face row
+// (32 lanes per row of the face box) and its lanes stride over x; taps come
+// from the binary32 shadow.
 template <int AX>
 __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, int phase) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (gated(&st[s], phase)) continue;
-    const long long n = face_box(I.g);
-    const double* u = cur(I, 1, parity);
-    const double* v = cur(I, 2, parity);
-    const double* w = cur(I, 3, parity);
+    const Geom& g = I.g;
+    const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1);
     double* tu = cur(I, 5, parity);
     double* tv = cur(I, 6, parity);
     double* tw = cur(I, 7, parity);
     FOR_ELEMS(tab)
-    if (el >= n) break;
-    int c, x, y, z;
-    if (face_of(I, el, &c, &x, &y, &z) && !mx_sweep_face<AX>(I.g, u, v, w, tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
-        atomicMin(&st[s].fault_gate, st[s].step * 8u + (unsigned)phase);
-        atomicMin(&st[s].fault_key, fault_key(c, x, y, z));
-    }
+    const long long row = el >> 5;
+    if (row >= rows) break;
+    const int lane = (int)(el & 31);
+    const unsigned r = (unsigned)row, r2 = I.ffy.div(r), cc = I.ffz.div(r2);
+    const int c = (int)cc;
+    const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
+    if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
+    const int x1 = g.G + g.NX + (c == 0);
+    for (int x = g.G + lane; x < x1; x += 32)
+        if (!mx_sweep_face<AX, float>(g, I.sh[0], I.sh[1], I.sh[2], tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
+            atomicMin(&st[s].fault_gate, st[s].step * 8u + (unsigned)phase);
+            atomicMin(&st[s].fault_key, fault_key(c, x, y, z));
+        }
     END_ELEMS
     END_TILES
 }
@@ -429,26 +456,41 @@ __device__ __forceinline__ float mg_interp(float ax, float ay, float az, float e
     return __fmaf_rn(bz, z1, __fmul_rn(az, z0));
 }
 
+// One red-black colour sweep of L e = r in place.  A warp owns one (y, z) row
+// and its lanes stride over the row's cells of the colour; the neighbour
+// rows are addressed through pointers clamped to the row itself at the
+// walls (the Neumann reflection, the same values as per-cell selects), so a
+// cell costs its eight loads, the relaxation and a store.  The iteration
+// space counts 32 lanes per row (row_box).
+__host__ __device__ inline long long row_box(const Lvl& L) { return 32ll * L.ny * L.nz; }
+
 __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color) {
     FOR_TILES(tab)
     if (ctl[s].stopped) continue;
     const Lvl L = inst[s].lev[l];
-    const int hx = (L.nx + 1) / 2;
-    const long long n = (long long)hx * L.ny * L.nz;
+    const long long rows = (long long)L.ny * L.nz;
     const long long nxy = (long long)L.nx * L.ny;
     const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
     FOR_ELEMS(tab)
-    if (el >= n) break;
-    const unsigned e = (unsigned)el, r = L.fhx.div(e), zz = L.fny.div(r);
-    const int k = (int)(e - r * (unsigned)hx), y = (int)(r - zz * (unsigned)L.ny), z = (int)zz;
-    const int x = (((y + z) & 1) != color ? 1 : 0) + 2 * k;
-    if (x < L.nx) {
-        const long long i = lidx(x, y, z, L.nx, L.ny);
-        const float c = L.e[i];
-        const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c);
-        const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c);
-        const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c);
-        L.e[i] = mg_relax(L, sx, sy, sz, L.r[i], inv, c);
+    const long long row = el >> 5;
+    if (row >= rows) break;
+    const int lane = (int)(el & 31);
+    const unsigned zz = L.fny.div((unsigned)row);
+    const int y = (int)((unsigned)row - zz * (unsigned)L.ny), z = (int)zz;
+    float* __restrict__ e = L.e + (long long)L.nx * y + nxy * z;
+    const float* __restrict__ rr = L.r + (long long)L.nx * y + nxy * z;
+    const float* ym = y > 0 ? e - L.nx : e;
+    const float* yp = y < L.ny - 1 ? e + L.nx : e;
+    const float* zm = z > 0 ? e - nxy : e;
+    const float* zp = z < L.nz - 1 ? e + nxy : e;
+    const int p = ((y + z) & 1) != color ? 1 : 0;
+    for (int x = p + 2 * lane; x < L.nx; x += 64) {
+        const int xm = x > 0 ? x - 1 : x, xp = x < L.nx - 1 ? x + 1 : x;
+        const float c = e[x];
+        const float sx = e[xm] + e[xp];
+        const float sy = ym[x] + yp[x];
+        const float sz = zm[x] + zp[x];
+        e[x] = mg_relax(L, sx, sy, sz, rr[x], inv, c);
     }
     END_ELEMS
     END_TILES
@@ -464,7 +506,8 @@ __device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) 
     return mg_res(L, sx, sy, sz, c, L.r[i]);
 }
 
-// Coarse rhs = mean of the children's residuals; coarse solution = 0.
+// Coarse rhs = mean of the children's residuals; coarse solution = 0.  One
+// thread per coarse cell (row-wise forms of this kernel measured slower).
 __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
     FOR_TILES(tab)
     if (ctl[s].stopped) continue;
@@ -489,25 +532,36 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l)
 
 // e_fine += cell-centred trilinear interpolation of e_coarse: per coarsened
 // axis the parent weighs 3/4 and the next coarse cell toward the fine cell
-// 1/4 (clamped at the walls, the Neumann reflection).
+// 1/4 (clamped at the walls, the Neumann reflection).  A warp owns one fine
+// (y, z) row (row_box of the fine level); its four coarse rows are fixed.
 __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
     FOR_TILES(tab)
     if (ctl[s].stopped) continue;
     const Lvl F = inst[s].lev[l];
     const Lvl C = inst[s].lev[l + 1];
-    const long long n = lvl_cells(F);
+    const long long rows = (long long)F.ny * F.nz;
     FOR_ELEMS(tab)
-    if (el >= n) break;
-    const unsigned e = (unsigned)el, r = F.fnx.div(e), zz = F.fny.div(r);
-    const int x = (int)(e - r * (unsigned)F.nx), y = (int)(r - zz * (unsigned)F.ny), z = (int)zz;
-    int X0 = x, X1 = x, Y0 = y, Y1 = y, Z0 = z, Z1 = z;
-    float ax = 1.0f, ay = 1.0f, az = 1.0f;
-    if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
+    const long long row = el >> 5;
+    if (row >= rows) break;
+    const int lane = (int)(el & 31);
+    const unsigned zz = F.fny.div((unsigned)row);
+    const int y = (int)((unsigned)row - zz * (unsigned)F.ny), z = (int)zz;
+    int Y0 = y, Y1 = y, Z0 = z, Z1 = z;
+    float ay = 1.0f, az = 1.0f;
     if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
     if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
-    auto E = [&](int i, int j, int k) { return C.e[lidx(i, j, k, C.nx, C.ny)]; };
-    F.e[el] = __fadd_rn(F.e[el], mg_interp(ax, ay, az, E(X0, Y0, Z0), E(X1, Y0, Z0), E(X0, Y1, Z0), E(X1, Y1, Z0),
-                                           E(X0, Y0, Z1), E(X1, Y0, Z1), E(X0, Y1, Z1), E(X1, Y1, Z1)));
+    const float* c00 = C.e + lidx(0, Y0, Z0, C.nx, C.ny);
+    const float* c10 = C.e + lidx(0, Y1, Z0, C.nx, C.ny);
+    const float* c01 = C.e + lidx(0, Y0, Z1, C.nx, C.ny);
+    const float* c11 = C.e + lidx(0, Y1, Z1, C.nx, C.ny);
+    float* fe = F.e + lidx(0, y, z, F.nx, F.ny);
+    for (int x = lane; x < F.nx; x += 32) {
+        int X0 = x, X1 = x;
+        float ax = 1.0f;
+        if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
+        fe[x] = __fadd_rn(fe[x], mg_interp(ax, ay, az, c00[X0], c00[X1], c10[X0], c10[X1], c01[X0], c01[X1], c11[X0],
+                                           c11[X1]));
+    }
     END_ELEMS
     END_TILES
 }
@@ -530,18 +584,23 @@ __device__ float block_sum(float v, float* red) {
 }
 
 // --- fused red-black pair ---------------------------------------------------
-// One red sweep then one black sweep of L e = r, from e_in into e_out: the
+// One red sweep then one black sweep of L e = r, from e_in into e_out.  The
 // red values read only e_in (their black neighbours are unchanged by the red
-// sweep), the black values read the new red values, which each block
-// computes for its x-y tile plus a one-cell halo into a ring of three planes
-// while it marches over a chunk of z-planes (the chunk's first red plane and
-// the one below it are recomputed).  Nothing reads what the kernel writes, so
-// blocks never race and the result equals the two in-place colour sweeps.
-constexpr int kPairTX = 32, kPairTY = 8, kPairZC = 32;
+// sweep); the black values read the new red values.  Each block owns an
+// output tile of kPairTX x kPairTY x kPairTZ cells: it first computes the new
+// red values of the tile plus a one-cell halo into shared memory (one
+// barrier), then writes every cell of the tile: red ones from shared memory,
+// black ones from their red neighbours there.  Nothing reads what the kernel
+// writes, so blocks never race, and the result equals the two in-place colour
+// sweeps bit for bit (the arithmetic is mg_relax in both).  Per pair it moves
+// e and r once and writes e once (12 B per cell) where the two colour
+// launches move about twice that.
+constexpr int kPairTX = 32, kPairTY = 8, kPairTZ = 4;
+constexpr int kPairHX = kPairTX + 2, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
 
 __global__ void __launch_bounds__(kPairTX * kPairTY) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab,
                                                                     int l, int dir) {
-    __shared__ float ring[3][kPairTY + 2][kPairTX + 2];
+    __shared__ float red[kPairHZ][kPairHY][kPairHX];
     const int tid = threadIdx.x + kPairTX * threadIdx.y;
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
@@ -556,50 +615,47 @@ __global__ void __launch_bounds__(kPairTX * kPairTY) kb_smooth_pair(const InstDe
         local /= ntx;
         const int by = local % nty;
         const int bz = local / nty;
-        const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairZC;
-        const int z1 = min(z0 + kPairZC, L.nz);
+        const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairTZ;
         const long long nxy = (long long)L.nx * L.ny;
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        auto red_plane = [&](int z, float (*dst)[kPairTX + 2]) {
-            for (int q = tid; q < (kPairTX + 2) * (kPairTY + 2); q += kPairTX * kPairTY) {
-                const int hx = q % (kPairTX + 2), hy = q / (kPairTX + 2);
-                const int x = x0 - 1 + hx, y = y0 - 1 + hy;
-                float v = 0.0f;
-                if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && ((x + y + z) & 1) == 0) {
-                    const long long i = x + (long long)L.nx * y + nxy * z;
-                    const float c = ein[i];
-                    const float sx = (x > 0 ? ein[i - 1] : c) + (x < L.nx - 1 ? ein[i + 1] : c);
-                    const float sy = (y > 0 ? ein[i - L.nx] : c) + (y < L.ny - 1 ? ein[i + L.nx] : c);
-                    const float sz = (z > 0 ? ein[i - nxy] : c) + (z < L.nz - 1 ? ein[i + nxy] : c);
-                    v = mg_relax(L, sx, sy, sz, r[i], inv, c);
-                }
-                dst[hy][hx] = v;
-            }
-        };
-        if (z0 > 0) red_plane(z0 - 1, ring[(z0 + 2) % 3]);
-        red_plane(z0, ring[z0 % 3]);
-        for (int z = z0; z < z1; ++z) {
-            if (z + 1 < L.nz) red_plane(z + 1, ring[(z + 1) % 3]);
-            __syncthreads();
-            const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
-            if (x < L.nx && y < L.ny) {
-                const int hx = threadIdx.x + 1, hy = threadIdx.y + 1;
+        for (int q = tid; q < kPairHX * kPairHY * kPairHZ; q += kPairTX * kPairTY) {
+            const int hx = q % kPairHX, t = q / kPairHX, hy = t % kPairHY, hz = t / kPairHY;
+            const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+            float v = 0.0f;
+            if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && z >= 0 && z < L.nz && ((x + y + z) & 1) == 0) {
                 const long long i = x + (long long)L.nx * y + nxy * z;
-                const float(*cp)[kPairTX + 2] = ring[z % 3];
+                const float c = ein[i];
+                const float sx = (x > 0 ? ein[i - 1] : c) + (x < L.nx - 1 ? ein[i + 1] : c);
+                const float sy = (y > 0 ? ein[i - L.nx] : c) + (y < L.ny - 1 ? ein[i + L.nx] : c);
+                const float sz = (z > 0 ? ein[i - nxy] : c) + (z < L.nz - 1 ? ein[i + nxy] : c);
+                v = mg_relax(L, sx, sy, sz, r[i], inv, c);
+            }
+            red[hz][hy][hx] = v;
+        }
+        __syncthreads();
+        const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+        if (x < L.nx && y < L.ny) {
+            const int hx = threadIdx.x + 1, hy = threadIdx.y + 1;
+#pragma unroll
+            for (int k = 0; k < kPairTZ; ++k) {
+                const int z = z0 + k;
+                if (z >= L.nz) break;
+                const int hz = k + 1;
+                const long long i = x + (long long)L.nx * y + nxy * z;
                 float out;
                 if (((x + y + z) & 1) == 0) {
-                    out = cp[hy][hx];
+                    out = red[hz][hy][hx];
                 } else {
                     const float c = ein[i];
-                    const float sx = (x > 0 ? cp[hy][hx - 1] : c) + (x < L.nx - 1 ? cp[hy][hx + 1] : c);
-                    const float sy = (y > 0 ? cp[hy - 1][hx] : c) + (y < L.ny - 1 ? cp[hy + 1][hx] : c);
-                    const float sz = (z > 0 ? ring[(z + 2) % 3][hy][hx] : c) + (z < L.nz - 1 ? ring[(z + 1) % 3][hy][hx] : c);
+                    const float sx = (x > 0 ? red[hz][hy][hx - 1] : c) + (x < L.nx - 1 ? red[hz][hy][hx + 1] : c);
+                    const float sy = (y > 0 ? red[hz][hy - 1][hx] : c) + (y < L.ny - 1 ? red[hz][hy + 1][hx] : c);
+                    const float sz = (z > 0 ? red[hz - 1][hy][hx] : c) + (z < L.nz - 1 ? red[hz + 1][hy][hx] : c);
                     out = mg_relax(L, sx, sy, sz, r[i], inv, c);
                 }
                 eout[i] = out;
             }
-            __syncthreads();
         }
+        __syncthreads();
     }
 }
 
@@ -934,7 +990,9 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     const long long per = (long long)sh.tpb * sh.ept;
     long long n = 0;
     if (st == S_BC) n = bc_count(I.g);
-    else if (st == S_SWEEP || st == S_GRAD) n = face_box(I.g);
+    else if (st == S_SWEEP) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
+    else if (st == S_GRAD) n = face_box(I.g);
+    else if (st == S_SHADOW) n = I.g.u.count + I.g.v.count + I.g.w.count;
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
     else if (st == S_PBC) n = pbc_count(I.g);
@@ -944,21 +1002,21 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
         // n set above
     } else if (st < S_RESTRICT) {
         const int l = st - S_SMOOTH;
-        n = (l < lim && !I.lev[l].e2) ? half_box(I.lev[l]) : 0;
+        n = (l < lim && !I.lev[l].e2) ? row_box(I.lev[l]) : 0;
     } else if (st >= S_RESTRICT && st < S_PROLONG) {
         const int l = st - S_RESTRICT;
         n = l < lim ? lvl_cells(I.lev[l + 1]) : 0;
     } else if (st >= S_PROLONG && st < S_BIGCOARSE) {
         const int l = st - S_PROLONG;
-        n = l < lim ? lvl_cells(I.lev[l]) : 0;
+        n = l < lim ? row_box(I.lev[l]) : 0;
     } else if (st >= S_BIGCOARSE && st < S_PAIR) {
         const int l = st - S_BIGCOARSE;
-        n = (l == I.nlev - 1 && I.tail < 0) ? half_box(I.lev[l]) : 0;
+        n = (l == I.nlev - 1 && I.tail < 0) ? row_box(I.lev[l]) : 0;
     } else if (st >= S_PAIR && st < S_COUNT) {
         const int l = st - S_PAIR;
         if (l >= lim || !I.lev[l].e2) return 0;
         const Lvl& L = I.lev[l];
-        return cdivl(L.nx, kPairTX) * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairZC);
+        return cdivl(L.nx, kPairTX) * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairTZ);
     }
     return cdivl(n, per);
 }
@@ -1018,6 +1076,7 @@ void rec(Batch* b, int idx, cudaStream_t s) {
 void enq_bc(Batch* b, int parity, int gate, cudaStream_t s) { LAUNCH(b, S_BC, kb_bc, b->d_inst, b->d_st, tab(b, S_BC), parity, gate); }
 
 void enq_sweep(Batch* b, int axis, int parity, int phase, cudaStream_t s) {
+    LAUNCH(b, S_SHADOW, kb_shadow, b->d_inst, tab(b, S_SHADOW), parity);
     const Tab t = tab(b, S_SWEEP);
     if (axis == 0) LAUNCH(b, S_SWEEP, kb_sweep<0>, b->d_inst, b->d_st, t, parity, phase);
     else if (axis == 1) LAUNCH(b, S_SWEEP, kb_sweep<1>, b->d_inst, b->d_st, t, parity, phase);
@@ -1337,6 +1396,8 @@ size_t batch_slot_bytes(const af_config& c) {
     fdesc(&off, cx, cy, cz + 1);
     const size_t arena = ((size_t)off + 255) & ~(size_t)255;
     const size_t bb = ((size_t)(cx * cy * cz) * 8 + 255) & ~(size_t)255;
+    auto al = [](int64_t n) { return ((size_t)n * 4 + 255) & ~(size_t)255; };
+    const size_t shb = al((cx + 1) * cy * cz) + al(cx * (cy + 1) * cz) + al(cx * cy * (cz + 1));
     Lvl lev[kMaxLev];
     int cs = 0, tf = 0;
     const int nl = plan_levels((int)c.nx, (int)c.ny, (int)c.nz, lev, &cs);
@@ -1344,7 +1405,7 @@ size_t batch_slot_bytes(const af_config& c) {
     const int lim = tail >= 0 ? tail : nl - 1;
     size_t mg = 0;
     for (int l = 0; l < nl; ++l) mg += ((l < lim && c.inner_sweeps % 2 == 0) ? 3 : 2) * (size_t)lvl_cells(lev[l]) * sizeof(float);
-    return arena + bb + ((mg + 255) & ~(size_t)255);
+    return arena + bb + shb + ((mg + 255) & ~(size_t)255);
 }
 
 int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
@@ -1408,12 +1469,14 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     const bool fused = c.inner_sweeps % 2 == 0 && batch_nu % 2 == 0 && b->pairs;
     const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
     const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
+    size_t sh_bytes[3];
+    for (int k = 0; k < 3; ++k) sh_bytes[k] = ((size_t)S.desc[1 + k].count * 4 + 255) & ~(size_t)255;
     size_t mg = 0;
     for (int l = 0; l < I.nlev; ++l)
         mg += ((l < lim && fused) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
     mg = (mg + 255) & ~(size_t)255;
     S.external_arena = arena != nullptr;
-    S.mem_bytes = (arena ? 0 : arena_bytes) + b_bytes + mg;
+    S.mem_bytes = (arena ? 0 : arena_bytes) + b_bytes + sh_bytes[0] + sh_bytes[1] + sh_bytes[2] + mg;
     if (b->use_pool) {
         S.mem = b->pool.alloc(S.mem_bytes);
         if (!S.mem) {
@@ -1437,6 +1500,10 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     for (int f = 0; f < 8; ++f) I.slot[f] = (double*)(base + S.desc[f].off);
     I.b = (double*)p;
     p += b_bytes;
+    for (int k = 0; k < 3; ++k) {
+        I.sh[k] = (float*)p;
+        p += sh_bytes[k];
+    }
     float* fp = (float*)p;
     for (int l = 0; l < I.nlev; ++l) {
         const long long n = lvl_cells(I.lev[l]);
@@ -1728,6 +1795,7 @@ std::string batch_tune(Batch* b, int reps) {
         const int gsz = grid(b, st), tpb = b->shape[st].tpb;
         if (st == S_BC) kb_bc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
         else if (st == S_SWEEP) kb_sweep<0><<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st == S_SHADOW) kb_shadow<<<gsz, tpb, 0, s>>>(b->d_inst, t, 0);
         else if (st == S_DIV) kb_div<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
         else if (st == S_INT) kb_residual<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, t, 0, 0);
         else if (st == S_PBC) kb_pbc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0);
@@ -1738,7 +1806,7 @@ std::string batch_tune(Batch* b, int reps) {
         else if (st >= S_PROLONG && st < S_BIGCOARSE)
             kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG);
     };
-    std::vector<int> stages = {S_BC, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD};
+    std::vector<int> stages = {S_BC, S_SHADOW, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD};
     for (int l = 0; l + 1 < L; ++l) {
         stages.push_back(S_SMOOTH + l);
         stages.push_back(S_RESTRICT + l);

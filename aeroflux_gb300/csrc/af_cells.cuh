@@ -299,12 +299,17 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 // --- binary32 advection + diffusion of one face (stencil.go:44-225) --------
 // Returns false on a NaN backtrace (a contained fault); the face is then not
 // written.  Only the active axis is interpolated: the other two weights are 0.
-template <int AX>
-__device__ __forceinline__ float mx_face_vel(const Geom& g, const double* u, const double* v, const double* w, int c,
-                                             int x, int y, int z) {
-    auto U = [&](int i, int j, int k) { return f64_to_f32(u[i + j * g.u.sy + k * g.u.sz]); };
-    auto V = [&](int i, int j, int k) { return f64_to_f32(v[i + j * g.v.sy + k * g.v.sz]); };
-    auto W = [&](int i, int j, int k) { return f64_to_f32(w[i + j * g.w.sy + k * g.w.sz]); };
+// Taps come from the binary64 fields (converted here) or from their binary32
+// shadow (converted once per sweep by the same f64_to_f32): the same values.
+__device__ __forceinline__ float tap32(const double* p, long long i) { return f64_to_f32(p[i]); }
+__device__ __forceinline__ float tap32(const float* p, long long i) { return p[i]; }
+
+template <int AX, class T>
+__device__ __forceinline__ float mx_face_vel(const Geom& g, const T* u, const T* v, const T* w, int c, int x, int y,
+                                             int z) {
+    auto U = [&](int i, int j, int k) { return tap32(u, i + j * g.u.sy + k * g.u.sz); };
+    auto V = [&](int i, int j, int k) { return tap32(v, i + j * g.v.sy + k * g.v.sz); };
+    auto W = [&](int i, int j, int k) { return tap32(w, i + j * g.w.sy + k * g.w.sz); };
     if (c == 0) {
         if (AX == 0) return U(x, y, z);
         if (AX == 1) return 0.25f * (V(x - 1, y, z) + V(x, y, z) + V(x - 1, y + 1, z) + V(x, y + 1, z));
@@ -320,14 +325,14 @@ __device__ __forceinline__ float mx_face_vel(const Geom& g, const double* u, con
     }
 }
 
-template <int AX>
-__device__ __forceinline__ bool mx_sweep_face(const Geom& g, const double* u, const double* v, const double* w,
-                                              double* tu, double* tv, double* tw, float dt_invh, float lam, int c,
-                                              int x, int y, int z) {
+template <int AX, class T>
+__device__ __forceinline__ bool mx_sweep_face(const Geom& g, const T* u, const T* v, const T* w, double* tu,
+                                              double* tv, double* tw, float dt_invh, float lam, int c, int x, int y,
+                                              int z) {
     const Dims& d = c == 0 ? g.u : (c == 1 ? g.v : g.w);
-    const double* sd = c == 0 ? u : (c == 1 ? v : w);
+    const T* sd = c == 0 ? u : (c == 1 ? v : w);
     double* dd = c == 0 ? tu : (c == 1 ? tv : tw);
-    const float vel = mx_face_vel<AX>(g, u, v, w, c, x, y, z);
+    const float vel = mx_face_vel<AX, T>(g, u, v, w, c, x, y, z);
     // Backtrace relative to the face, so binary32 keeps the fraction accurate
     // at any grid size: departure = face + off, off = -dt*v/h.
     const int ca = AX == 0 ? x : (AX == 1 ? y : z);
@@ -352,12 +357,12 @@ __device__ __forceinline__ bool mx_sweep_face(const Geom& g, const double* u, co
     const long long s = AX == 0 ? 1 : (AX == 1 ? d.sy : d.sz);
     const long long base = (long long)x + (long long)y * d.sy + (long long)z * d.sz;
     const long long j0 = base + (long long)(i0 - ca) * s;
-    const float d0 = f64_to_f32(sd[j0]), d1 = f64_to_f32(sd[j0 + s]);
+    const float d0 = tap32(sd, j0), d1 = tap32(sd, j0 + s);
     const float adv = fmaf(t, d1 - d0, d0);
     float lap = 0.0f;
     if (lam != 0.0f) {
-        const float c0 = f64_to_f32(sd[base]);
-        lap = lam * ((f64_to_f32(sd[base - s]) - 2.0f * c0) + f64_to_f32(sd[base + s]));
+        const float c0 = tap32(sd, base);
+        lap = lam * ((tap32(sd, base - s) - 2.0f * c0) + tap32(sd, base + s));
     }
     dd[base] = f32_to_f64(adv + lap);
     return true;
