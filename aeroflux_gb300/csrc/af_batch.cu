@@ -587,21 +587,21 @@ __device__ float block_sum(float v, float* red) {
 // One red sweep then one black sweep of L e = r, from e_in into e_out.  The
 // red values read only e_in (their black neighbours are unchanged by the red
 // sweep); the black values read the new red values.  Each block owns an
-// output tile of kPairTX x kPairTY x kPairTZ cells: it first computes the new
-// red values of the tile plus a one-cell halo into shared memory (one
-// barrier), then writes every cell of the tile: red ones from shared memory,
-// black ones from their red neighbours there.  Nothing reads what the kernel
-// writes, so blocks never race, and the result equals the two in-place colour
-// sweeps bit for bit (the arithmetic is mg_relax in both).  Per pair it moves
-// e and r once and writes e once (12 B per cell) where the two colour
-// launches move about twice that.
-constexpr int kPairTX = 32, kPairTY = 8, kPairTZ = 4;
-constexpr int kPairHX = kPairTX + 2, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
+// output tile of kPairTX x kPairTY x kPairTZ cells.  It first computes the
+// new red values of the tile plus a one-cell halo -- only the red cells, kept
+// compactly in shared memory (a row of the halo alternates colours, so
+// x >> 1 indexes its red cells) -- then, after one barrier, each lane writes
+// an adjacent (x, x+1) pair of the tile, one red cell (from shared memory)
+// and one black cell (from its red neighbours there), so lanes never diverge
+// on colour.  Nothing reads what the kernel writes, so blocks never race, and
+// the result equals the two in-place colour sweeps bit for bit (mg_relax in
+// both).  Per pair it moves e and r once and writes e once.
+constexpr int kPairTX = 64, kPairTY = 8, kPairTZ = 8;
+constexpr int kPairRX = kPairTX / 2 + 1, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
 
-__global__ void __launch_bounds__(kPairTX * kPairTY) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab,
-                                                                    int l, int dir) {
-    __shared__ float red[kPairHZ][kPairHY][kPairHX];
-    const int tid = threadIdx.x + kPairTX * threadIdx.y;
+__global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir) {
+    __shared__ float red[kPairHZ][kPairHY][kPairRX];
+    const int tid = threadIdx.x;
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (ctl[s].stopped) continue;
@@ -618,41 +618,51 @@ __global__ void __launch_bounds__(kPairTX * kPairTY) kb_smooth_pair(const InstDe
         const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairTZ;
         const long long nxy = (long long)L.nx * L.ny;
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        for (int q = tid; q < kPairHX * kPairHY * kPairHZ; q += kPairTX * kPairTY) {
-            const int hx = q % kPairHX, t = q / kPairHX, hy = t % kPairHY, hz = t / kPairHY;
-            const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+        // Red cells of the halo tile: halo x = x0 - 1 + hx with hx = 2k +
+        // ((y + z + 1) & 1), k < kPairRX = 33.  One warp per halo row (hy, hz)
+        // takes k < 32; the rows' last cells (k = 32) go one per thread.
+        auto red_cell = [&](int hy, int hz, int k) {
+            const int y = y0 - 1 + hy, z = z0 - 1 + hz;
+            const int x = x0 - 1 + 2 * k + ((y + z + 1) & 1);
             float v = 0.0f;
-            if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && z >= 0 && z < L.nz && ((x + y + z) & 1) == 0) {
-                const long long i = x + (long long)L.nx * y + nxy * z;
-                const float c = ein[i];
-                const float sx = (x > 0 ? ein[i - 1] : c) + (x < L.nx - 1 ? ein[i + 1] : c);
-                const float sy = (y > 0 ? ein[i - L.nx] : c) + (y < L.ny - 1 ? ein[i + L.nx] : c);
-                const float sz = (z > 0 ? ein[i - nxy] : c) + (z < L.nz - 1 ? ein[i + nxy] : c);
-                v = mg_relax(L, sx, sy, sz, r[i], inv, c);
+            if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && z >= 0 && z < L.nz) {
+                const long long ro = (long long)L.nx * y + nxy * z;
+                const float* row_e = ein + ro;
+                const float* ym = y > 0 ? row_e - L.nx : row_e;
+                const float* yp = y < L.ny - 1 ? row_e + L.nx : row_e;
+                const float* zm = z > 0 ? row_e - nxy : row_e;
+                const float* zp = z < L.nz - 1 ? row_e + nxy : row_e;
+                const int xm = x > 0 ? x - 1 : x, xp = x < L.nx - 1 ? x + 1 : x;
+                v = mg_relax(L, row_e[xm] + row_e[xp], ym[x] + yp[x], zm[x] + zp[x], r[ro + x], inv, row_e[x]);
             }
-            red[hz][hy][hx] = v;
-        }
+            red[hz][hy][k] = v;
+        };
+        for (int row = tid >> 5; row < kPairHY * kPairHZ; row += 8) red_cell(row % kPairHY, row / kPairHY, tid & 31);
+        for (int row = tid; row < kPairHY * kPairHZ; row += 256) red_cell(row % kPairHY, row / kPairHY, kPairRX - 1);
         __syncthreads();
-        const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
-        if (x < L.nx && y < L.ny) {
-            const int hx = threadIdx.x + 1, hy = threadIdx.y + 1;
-#pragma unroll
-            for (int k = 0; k < kPairTZ; ++k) {
-                const int z = z0 + k;
+        // Output pairs: lane -> x = x0 + 2*lane + {0, 1}, warp -> y, loop over z.
+        const int lane = tid & 31, ty = tid >> 5;
+        const int y = y0 + ty, hy = ty + 1;
+        const int xa = x0 + 2 * lane;
+        if (y < L.ny && xa < L.nx) {
+            for (int tz = 0; tz < kPairTZ; ++tz) {
+                const int z = z0 + tz;
                 if (z >= L.nz) break;
-                const int hz = k + 1;
-                const long long i = x + (long long)L.nx * y + nxy * z;
-                float out;
-                if (((x + y + z) & 1) == 0) {
-                    out = red[hz][hy][hx];
-                } else {
-                    const float c = ein[i];
-                    const float sx = (x > 0 ? red[hz][hy][hx - 1] : c) + (x < L.nx - 1 ? red[hz][hy][hx + 1] : c);
-                    const float sy = (y > 0 ? red[hz][hy - 1][hx] : c) + (y < L.ny - 1 ? red[hz][hy + 1][hx] : c);
-                    const float sz = (z > 0 ? red[hz - 1][hy][hx] : c) + (z < L.nz - 1 ? red[hz + 1][hy][hx] : c);
-                    out = mg_relax(L, sx, sy, sz, r[i], inv, c);
+                const int hz = tz + 1;
+                const long long ro = (long long)L.nx * y + nxy * z;
+                // Of the pair, the red cell is xa + pr, the black one xa + 1 - pr.
+                const int pr = (xa + y + z) & 1;
+                const int xr = xa + pr, xb = xa + 1 - pr;
+                // Halo x index h = x - x0 + 1; red cell h >> 1 in its row.
+                if (xr < L.nx) eout[ro + xr] = red[hz][hy][(xr - x0 + 1) >> 1];
+                if (xb < L.nx) {
+                    const int h = xb - x0 + 1;
+                    const float c = ein[ro + xb];
+                    const float sx = (xb > 0 ? red[hz][hy][(h - 1) >> 1] : c) + (xb < L.nx - 1 ? red[hz][hy][(h + 1) >> 1] : c);
+                    const float sy = (y > 0 ? red[hz][hy - 1][h >> 1] : c) + (y < L.ny - 1 ? red[hz][hy + 1][h >> 1] : c);
+                    const float sz = (z > 0 ? red[hz - 1][hy][h >> 1] : c) + (z < L.nz - 1 ? red[hz + 1][hy][h >> 1] : c);
+                    eout[ro + xb] = mg_relax(L, sx, sy, sz, r[ro + xb], inv, c);
                 }
-                eout[i] = out;
             }
         }
         __syncthreads();
@@ -934,7 +944,7 @@ struct Batch {
     size_t tail_smem = 0;            // dynamic shared memory of the tail V-cycle
     int graph_nu = 0;                // smoothing sweeps the captured graph carries
     bool per_level = false;          // multigrid without the tail V-cycle above the coarsest level
-    bool pairs = false;              // fused red-black pair smoothing below the tail
+    bool pairs = true;               // fused red-black pair smoothing below the tail
     cudaGraphExec_t graph = nullptr;
     bool tables_dirty = true;
     bool profiling = false;
@@ -1096,8 +1106,7 @@ void enq_smooth(Batch* b, int st, int l, int pairs, cudaStream_t s) {
 void enq_level_smooth(Batch* b, int l, cudaStream_t s) {
     if (b->graph_pair & (1u << l))
         for (int k = 0; k < b->nu; ++k) {
-            kb_smooth_pair<<<grid(b, S_PAIR + l), dim3(kPairTX, kPairTY), 0, s>>>(b->d_inst, b->d_ctl,
-                                                                                tab(b, S_PAIR + l), l, k & 1);
+            kb_smooth_pair<<<grid(b, S_PAIR + l), 256, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1);
             ++b->launches;
         }
     if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
@@ -1284,7 +1293,7 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     if (const char* fp = getenv("AEROFLUX_MG_PAIRS")) b->pairs = atoi(fp) != 0;
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
-    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{kPairTX * kPairTY, 1, 8};
+    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{256, 1, 8};
     cudaError_t rc;
     if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -1467,13 +1476,13 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
         if (i != s && b->slots[i].used) others = true;
     const int batch_nu = others ? b->nu : (int)c.inner_sweeps;
     const bool fused = c.inner_sweeps % 2 == 0 && batch_nu % 2 == 0 && b->pairs;
+    auto pair_level = [&](int l) { return fused && l < lim; };
     const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
     const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
     size_t sh_bytes[3];
     for (int k = 0; k < 3; ++k) sh_bytes[k] = ((size_t)S.desc[1 + k].count * 4 + 255) & ~(size_t)255;
     size_t mg = 0;
-    for (int l = 0; l < I.nlev; ++l)
-        mg += ((l < lim && fused) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
+    for (int l = 0; l < I.nlev; ++l) mg += (pair_level(l) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
     mg = (mg + 255) & ~(size_t)255;
     S.external_arena = arena != nullptr;
     S.mem_bytes = (arena ? 0 : arena_bytes) + b_bytes + sh_bytes[0] + sh_bytes[1] + sh_bytes[2] + mg;
@@ -1511,7 +1520,7 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
         I.lev[l].r = fp + n;
         fp += 2 * n;
         I.lev[l].e2 = nullptr;
-        if (l < lim && fused) {
+        if (pair_level(l)) {
             I.lev[l].e2 = fp;
             fp += n;
         }

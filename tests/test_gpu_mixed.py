@@ -61,15 +61,20 @@ def test_projection_reaches_tolerance_with_any_sweep_count(sweeps):
 
 
 def run_steps(n, steps, per_level, pairs):
+    """pairs: True, False or None (the library's default)."""
     env = {"AEROFLUX_MG_PER_LEVEL": "1" if per_level else "0", "AEROFLUX_MG_PAIRS": "1" if pairs else "0"}
-    old = {k: os.environ.get(k) for k in env}
+    if pairs is None:
+        del env["AEROFLUX_MG_PAIRS"]
+    old = {k: os.environ.get(k) for k in ("AEROFLUX_MG_PER_LEVEL", "AEROFLUX_MG_PAIRS")}
+    for k in old:
+        os.environ.pop(k, None)
     os.environ.update(env)
     try:
         e = seeded(mixed_cfg(n, DT=0.002))
     finally:
         for k, v in old.items():
             if v is None:
-                del os.environ[k]
+                os.environ.pop(k, None)
             else:
                 os.environ[k] = v
     e.Step(steps)
@@ -78,13 +83,14 @@ def run_steps(n, steps, per_level, pairs):
     return out
 
 
-@pytest.mark.parametrize("n", [(32, 32, 32), (48, 32, 96), (64, 64, 64), (33, 17, 20)])
+@pytest.mark.parametrize("n", [(32, 32, 32), (48, 32, 96), (64, 64, 64), (33, 17, 20), (160, 176, 144)])
 def test_fused_pairs_and_tail_vcycle_equal_per_level_kernels(n):
     # The fused red-black pair and the one-block tail V-cycle reorganise the
     # per-level colour sweeps without changing any rounding: identical bits.
     ref = run_steps(n, 2, True, False)
     assert np.array_equal(run_steps(n, 2, False, False), ref)
     assert np.array_equal(run_steps(n, 2, False, True), ref)
+    assert np.array_equal(run_steps(n, 2, False, None), ref)
 
 
 def test_projection_matches_converged_fp64_oracle():
