@@ -98,6 +98,7 @@ struct InstDev {
     FastDiv ffx, ffy, ffz;   // NX+1, NY+1, NZ+1 (the face box)
     FastDiv fnx, fny;        // NX, NY
     float* sh[3];            // binary32 shadow of the current U, V, W (the sweeps' taps)
+    int warm;                // 1: a projection starts from the last pressure, 0: from zero
     Lvl lev[kMaxLev];
 };
 
@@ -207,7 +208,7 @@ __global__ void kb_div(const InstDev* inst, Status* st, Tab tab, int parity, int
     if (el >= n) break;
     const unsigned e = (unsigned)el, r = I.fpx.div(e), z = I.fpy.div(r);
     div_cell(g, cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.slot[0], I.slot[4], I.b, I.div_scale,
-             I.h2, true, (int)(e - r * g.p.nx), (int)(r - z * g.p.ny), (int)z);
+             I.h2, !I.warm, (int)(e - r * g.p.nx), (int)(r - z * g.p.ny), (int)z);
     END_ELEMS
     END_TILES
 }
@@ -945,6 +946,7 @@ struct Batch {
     int graph_nu = 0;                // smoothing sweeps the captured graph carries
     bool per_level = false;          // multigrid without the tail V-cycle above the coarsest level
     bool pairs = true;               // fused red-black pair smoothing below the tail
+    bool cold = false;               // every projection starts from P = 0 (the reference's zeroing)
     cudaGraphExec_t graph = nullptr;
     bool tables_dirty = true;
     bool profiling = false;
@@ -1291,6 +1293,10 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     // level), and fused red-black pairs on or off: the same bits either way.
     if (const char* pl = getenv("AEROFLUX_MG_PER_LEVEL")) b->per_level = atoi(pl) != 0;
     if (const char* fp = getenv("AEROFLUX_MG_PAIRS")) b->pairs = atoi(fp) != 0;
+    // The refinement solves to a tolerance, so it may start from the last
+    // projection's pressure instead of zero (project.go:81-83 zeroes it for
+    // the fixed sweep count of the red-black solver).
+    if (const char* cs = getenv("AEROFLUX_COLD_START")) b->cold = atoi(cs) != 0;
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{256, 1, 8};
@@ -1537,6 +1543,7 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.thresh = 0.5 * c.div_tol;
     I.max_refine = (unsigned)c.max_refine;
     I.parity = 0;
+    I.warm = b->cold ? 0 : 1;
     // Smoothing sweeps per level are a property of the batch's step graph:
     // the first slot of an empty batch sets them.
     b->nu = batch_nu;
