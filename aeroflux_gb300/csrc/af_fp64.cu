@@ -102,6 +102,18 @@ __device__ __forceinline__ double lerp_t0(double a, double b) {
     return a;
 }
 
+// |v| < 2^1023 on the bit pattern: a lerp of two such values with weights in
+// [0, 1] is finite (the result is bounded by the larger magnitude times
+// (1-t) + t <= 1 + 2^-53), so it adds as an exact zero when its weight is +0.
+__device__ __forceinline__ bool below_2p1023(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7FF0000000000000ull) < 0x7FE0000000000000ull;
+}
+// Finite and nonzero: x + (+-0) == x and x * 1 == x exactly.
+__device__ __forceinline__ bool finite_nonzero(double v) {
+    const unsigned long long m = (unsigned long long)__double_as_longlong(v) & ~kSign;
+    return m != 0ull && m < 0x7FF0000000000000ull;
+}
+
 template <int AX>
 __global__ void k_sweep_fp64(SweepArgs a) {
     if (gated(a.st, a.phase)) return;
@@ -163,21 +175,39 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     const long long b = (long long)i000;
     // Only the active axis has a nonzero weight; the lerps along the other
     // two (weight exactly +0) run on the integer pipe with identical bits.
+    // The zero-weight lerps only matter when their operands are not finite
+    // (NaN propagates, Inf * 0 is NaN) or when the kept value is a zero
+    // (-0 + +0 = +0): otherwise the kept value passes through exactly, and
+    // the FP64 work of the discarded lerps is skipped.
     double adv;
     if (AX == 0) {
         const double omt = dsub(1.0, tx);
         const double c00 = lerp(sd[b], sd[b + 1], tx, omt);
-        const double c10 = lerp(sd[b + sy], sd[b + sy + 1], tx, omt);
-        const double c01 = lerp(sd[b + sz], sd[b + sz + 1], tx, omt);
-        const double c11 = lerp(sd[b + sz + sy], sd[b + sz + sy + 1], tx, omt);
-        adv = lerp_t0(lerp_t0(c00, c10), lerp_t0(c01, c11));
+        const double t1 = sd[b + sy], t2 = sd[b + sy + 1], t3 = sd[b + sz], t4 = sd[b + sz + 1];
+        const double t5 = sd[b + sz + sy], t6 = sd[b + sz + sy + 1];
+        if (finite_nonzero(c00) && below_2p1023(t1) && below_2p1023(t2) && below_2p1023(t3) && below_2p1023(t4) &&
+            below_2p1023(t5) && below_2p1023(t6)) {
+            adv = c00;
+        } else {
+            const double c10 = lerp(t1, t2, tx, omt);
+            const double c01 = lerp(t3, t4, tx, omt);
+            const double c11 = lerp(t5, t6, tx, omt);
+            adv = lerp_t0(lerp_t0(c00, c10), lerp_t0(c01, c11));
+        }
     } else if (AX == 1) {
         const double omt = dsub(1.0, ty);
         const double c00 = lerp_t0(sd[b], sd[b + 1]);
         const double c10 = lerp_t0(sd[b + sy], sd[b + sy + 1]);
-        const double c01 = lerp_t0(sd[b + sz], sd[b + sz + 1]);
-        const double c11 = lerp_t0(sd[b + sz + sy], sd[b + sz + sy + 1]);
-        adv = lerp_t0(lerp(c00, c10, ty, omt), lerp(c01, c11, ty, omt));
+        const double y0 = lerp(c00, c10, ty, omt);
+        const double t3 = sd[b + sz], t4 = sd[b + sz + 1], t5 = sd[b + sz + sy], t6 = sd[b + sz + sy + 1];
+        // lerp_t0 of values below 2^1023 is one of them or a zero: below too.
+        if (finite_nonzero(y0) && below_2p1023(t3) && below_2p1023(t4) && below_2p1023(t5) && below_2p1023(t6)) {
+            adv = y0;
+        } else {
+            const double c01 = lerp_t0(t3, t4);
+            const double c11 = lerp_t0(t5, t6);
+            adv = lerp_t0(y0, lerp(c01, c11, ty, omt));
+        }
     } else {
         const double c00 = lerp_t0(sd[b], sd[b + 1]);
         const double c10 = lerp_t0(sd[b + sy], sd[b + sy + 1]);

@@ -83,6 +83,58 @@ def test_sweep_bit_exact_with_garbage_halo(name):
     assert_bit_identical(gpu, orc, FIELDS, "three sweeps")
 
 
+EXTREMES = {
+    # 2^1023 = 8.98846567e307: the shortcut's threshold lies between the two.
+    "finite": [0.0, -0.0, 1.7e308, -1.7e308, 8.98e307, -8.98e307, 8.99e307, -8.99e307, 5e-324, -5e-324],
+    "inf": [0.0, -0.0, 1.7e308, -1.7e308, math.inf, -math.inf, 5e-324],
+}
+
+
+@pytest.mark.parametrize("name", ["tg12", "odd10x7x5", "rect33x17x20"])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+@pytest.mark.parametrize("kind", list(EXTREMES))
+def test_sweep_bit_exact_with_extreme_values(name, seed, kind):
+    # Signed zeros, magnitudes near the top of binary64 (zero-weight lerps
+    # of them overflow), infinities (clamped backtraces, Inf * 0 = NaN) and
+    # subnormals, planted among ordinary values in every field: the sweeps'
+    # shortcuts for zero-weight lerps must reproduce the reference in all of
+    # these cases.  A face velocity that averages +Inf with -Inf is NaN, a
+    # contained fault: then both must report the same fault (single-worker
+    # oracle order) and hold the same U, V, W.
+    cfg, _, _ = _cfg(name)
+    gpu = New(cfg)
+    kw = oracle_kwargs(cfg)
+    kw["workers"] = 1
+    orc = OracleEngine(**kw)
+    rng = np.random.default_rng(100 + seed)
+    specials = np.array(EXTREMES[kind])
+    for name_f in ("U", "V", "W"):
+        a = rng.normal(size=orc.field(FID[name_f]).count)
+        pick = rng.random(a.size) < 0.03
+        a[pick] = rng.choice(specials, size=int(pick.sum()))
+        zeros = rng.random(a.size) < 0.04
+        a[zeros] = rng.choice([0.0, -0.0], size=int(zeros.sum()))
+        orc.data(FID[name_f])[:] = a
+        gpu.upload(name_f, a)
+    dt = orc.cfg["dt"] * 0.5
+    for axis in (0, 1, 2):
+        ofault = gfault = None
+        try:
+            orc.sweep(axis, dt)
+        except OracleError as ex:
+            ofault = str(ex)
+        try:
+            gpu.sweep(axis, dt)
+        except FaultError as ex:
+            gfault = str(ex)
+        assert gfault == ofault
+        if ofault:
+            assert_bit_identical(gpu, orc, ["U", "V", "W"], f"state after the fault in sweep axis {axis}")
+            break
+        assert_bit_identical(gpu, orc, ["U", "V", "W", "Tmp0", "Tmp1", "Tmp2"], f"sweep axis {axis}")
+    orc.close()
+
+
 @pytest.mark.parametrize("name", list(SHAPES))
 def test_projection_stages_bit_exact(name):
     cfg, kind, amp = _cfg(name)
