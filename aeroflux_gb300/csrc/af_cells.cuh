@@ -21,6 +21,62 @@ __device__ __forceinline__ double flip(double a) {
     return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(a) ^ kSign));
 }
 
+// --- exact binary64 steps on the integer pipe ------------------------------
+// GB300's FP64 pipe (about two operations per SM per clock) also executes
+// binary64 compares and conversions; the sweeps move the exact ones here.
+constexpr unsigned long long kFrac = 0xFFFFFFFFFFFFFull;
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ double dfrom(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// (double)n for 0 <= n < 2^31.
+__device__ __forceinline__ double i2d_small(int n) {
+    if (n == 0) return 0.0;
+    const int lz = __clz(n);
+    return dfrom(((unsigned long long)(1023 + 31 - lz) << 52) | (((unsigned long long)(unsigned)n << (21 + lz)) & kFrac));
+}
+
+// Truncation toward zero of +-0 <= x < 2^31 (finite).
+__device__ __forceinline__ long long d2i_trunc_small(double x) {
+    const unsigned long long b = dbits(x) & ~kSign;
+    const int e = (int)(b >> 52) - 1023;
+    if (e < 0) return 0;
+    return (long long)(((b & kFrac) | (1ull << 52)) >> (52 - e));
+}
+
+// x - a0 for finite 0 <= x < 2^31 (or -0) and an integer a0 with
+// trunc(x) - 1 <= a0 <= trunc(x) and x - a0 <= 1: the exact difference (the
+// binary64 subtraction is exact here too), including -0 - 0 = -0.
+__device__ __forceinline__ double frac_sub(double x, long long a0) {
+    const unsigned long long b = dbits(x);
+    const int e = (int)((b & ~kSign) >> 52) - 1023;
+    if (e < 0) return a0 == 0 ? x : dsub(x, (double)a0);  // x < 1: a0 is 0 here
+    const unsigned long long m = (b & kFrac) | (1ull << 52);
+    const long long t = (long long)(m >> (52 - e));
+    if (t != a0) return 1.0;  // a0 = t - 1 only when x = t: difference 1
+    const unsigned long long f = m & ((1ull << (52 - e)) - 1ull);
+    if (f == 0) return 0.0;
+    const int p = 63 - __clzll((long long)f);  // leading bit of f, value f * 2^(e-52)
+    return dfrom(((unsigned long long)(1023 + e - 52 + p) << 52) | ((f << (52 - p)) & kFrac));
+}
+
+// RN(0.25 * x) and RN(2 * x): exact exponent shifts while the result stays
+// normal (and for 0, Inf, NaN, which pass through); the FP64 multiply
+// otherwise, so every input rounds as the multiply would.
+__device__ __forceinline__ double quarter(double x) {
+    const unsigned long long b = dbits(x);
+    const unsigned e = (unsigned)((b >> 52) & 0x7FF);
+    if (e >= 3u && e < 0x7FFu) return dfrom(b - (2ull << 52));
+    if (e == 0x7FFu || (b & ~kSign) == 0ull) return x;
+    return dmul(0.25, x);
+}
+__device__ __forceinline__ double twice(double x) {
+    const unsigned long long b = dbits(x);
+    const unsigned e = (unsigned)((b >> 52) & 0x7FF);
+    if (e >= 1u && e < 0x7FEu) return dfrom(b + (1ull << 52));
+    if (e == 0x7FFu || (b & ~kSign) == 0ull) return x;
+    return dmul(2.0, x);
+}
+
 // Correctly rounded x/6.  Because 6 = 3*2, x/6 is never within ulp/6 of a
 // rounding midpoint, while q + r*c below is within 2^-54 ulp of x/6 (q =
 // RN(x*RN(1/6)), r = x - 6q computed exactly by the FMA, RN(1/6) = (1-2^-54)/6).

@@ -67,18 +67,18 @@ __device__ __forceinline__ double face_vel(const SweepArgs& a, int c, int x, int
     if (c == 0) {
         if (AX == 0) return U(x, y, z);
         if (AX == 1)
-            return dmul(0.25, dadd(dadd(dadd(V(x - 1, y, z), V(x, y, z)), V(x - 1, y + 1, z)), V(x, y + 1, z)));
-        return dmul(0.25, dadd(dadd(dadd(W(x - 1, y, z), W(x, y, z)), W(x - 1, y, z + 1)), W(x, y, z + 1)));
+            return quarter(dadd(dadd(dadd(V(x - 1, y, z), V(x, y, z)), V(x - 1, y + 1, z)), V(x, y + 1, z)));
+        return quarter(dadd(dadd(dadd(W(x - 1, y, z), W(x, y, z)), W(x - 1, y, z + 1)), W(x, y, z + 1)));
     } else if (c == 1) {
         if (AX == 0)
-            return dmul(0.25, dadd(dadd(dadd(U(x, y - 1, z), U(x + 1, y - 1, z)), U(x, y, z)), U(x + 1, y, z)));
+            return quarter(dadd(dadd(dadd(U(x, y - 1, z), U(x + 1, y - 1, z)), U(x, y, z)), U(x + 1, y, z)));
         if (AX == 1) return V(x, y, z);
-        return dmul(0.25, dadd(dadd(dadd(W(x, y - 1, z), W(x, y, z)), W(x, y - 1, z + 1)), W(x, y, z + 1)));
+        return quarter(dadd(dadd(dadd(W(x, y - 1, z), W(x, y, z)), W(x, y - 1, z + 1)), W(x, y, z + 1)));
     } else {
         if (AX == 0)
-            return dmul(0.25, dadd(dadd(dadd(U(x, y, z - 1), U(x + 1, y, z - 1)), U(x, y, z)), U(x + 1, y, z)));
+            return quarter(dadd(dadd(dadd(U(x, y, z - 1), U(x + 1, y, z - 1)), U(x, y, z)), U(x + 1, y, z)));
         if (AX == 1)
-            return dmul(0.25, dadd(dadd(dadd(V(x, y, z - 1), V(x, y + 1, z - 1)), V(x, y, z)), V(x, y + 1, z)));
+            return quarter(dadd(dadd(dadd(V(x, y, z - 1), V(x, y + 1, z - 1)), V(x, y, z)), V(x, y + 1, z)));
         return W(x, y, z);
     }
 }
@@ -134,19 +134,22 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     // Backtrace along the active axis only: p -= dt*v*invH.
     const int ca = AX == 0 ? x : (AX == 1 ? y : z);
     const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
-    double pa = dsub((double)ca, dmul(dmul(a.dt, vel), a.invH));
-    const double maxA = (double)(na - 1);
-    if (pa < 0) pa = 0;
-    else if (pa > maxA) pa = maxA;
+    double pa = dsub(i2d_small(ca), dmul(dmul(a.dt, vel), a.invH));
+    // Clamp to [0, na-1] (pa < 0 and pa > maxA on the bit patterns: -0 and
+    // NaN pass through unchanged, as the comparisons leave them).
+    const unsigned long long pab = dbits(pa);
+    const bool pnan = (pab & ~kSign) > 0x7FF0000000000000ull;
+    if (!pnan) {
+        if ((pab & kSign) && (pab & ~kSign)) pa = 0.0;
+        else if (!(pab & kSign) && pab > dbits(i2d_small(na - 1))) pa = i2d_small(na - 1);
+    }
 
     // Truncation toward zero as amd64 CVTTSD2SQ does (NaN -> INT64_MIN).  The
     // two other coordinates are integer faces strictly inside the padded
     // field, so their floor is the face itself and their weight is +0.
-    long long a0;
-    if (isnan(pa)) a0 = (long long)0x8000000000000000ull;
-    else a0 = (long long)pa;
+    long long a0 = pnan ? (long long)0x8000000000000000ull : d2i_trunc_small(pa);
     if (a0 >= na - 1) a0 = na - 2;
-    const double ta = dsub(pa, (double)a0);
+    const double ta = pnan ? dsub(pa, (double)a0) : frac_sub(pa, a0);
     long long x0 = x, y0 = y, z0 = z;
     double tx = 0.0, ty = 0.0, tz = 0.0;
     if (AX == 0) { x0 = a0; tx = ta; }
@@ -156,7 +159,7 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     const unsigned long long i000 =
         (unsigned long long)x0 + (unsigned long long)y0 * (unsigned long long)d.sy +
         (unsigned long long)z0 * (unsigned long long)d.sz;
-    if (isnan(pa)) {
+    if (pnan) {
         // Only a NaN coordinate can leave the field; Go bounds-checks the taps
         // in source order and panics at the first out-of-range one.
         const unsigned long long sy = d.sy, sz = d.sz, n = d.count;
@@ -220,7 +223,7 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     double lap = 0.0;
     if (a.lam != 0) {
         const long long s = AX == 0 ? 1 : (AX == 1 ? sy : sz);
-        lap = dmul(a.lam, dadd(dsub(sd[i - s], dmul(2.0, sd[i])), sd[i + s]));
+        lap = dmul(a.lam, dadd(dsub(sd[i - s], twice(sd[i])), sd[i + s]));
     }
     dd[i] = dadd(adv, lap);
 }
