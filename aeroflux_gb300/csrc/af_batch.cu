@@ -602,7 +602,7 @@ constexpr int kPairRX = kPairTX / 2 + 1, kPairHY = kPairTY + 2, kPairHZ = kPairT
 
 __global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir) {
     __shared__ float red[kPairHZ][kPairHY][kPairRX];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (ctl[s].stopped) continue;
@@ -610,59 +610,55 @@ __global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const
         const float* __restrict__ ein = dir ? L.e2 : L.e;
         float* __restrict__ eout = dir ? L.e : L.e2;
         const float* __restrict__ r = L.r;
-        const int ntx = (L.nx + kPairTX - 1) / kPairTX, nty = (L.ny + kPairTY - 1) / kPairTY;
+        const int nx = L.nx, ny = L.ny, nz = L.nz, nxy = nx * ny;  // a level holds < 2^31 cells
+        const int ntx = (nx + kPairTX - 1) / kPairTX, nty = (ny + kPairTY - 1) / kPairTY;
         int local = item - tab.prefix[s];
         const int bx = local % ntx;
         local /= ntx;
         const int by = local % nty;
         const int bz = local / nty;
         const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairTZ;
-        const long long nxy = (long long)L.nx * L.ny;
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        // Red cells of the halo tile: halo x = x0 - 1 + hx with hx = 2k +
-        // ((y + z + 1) & 1), k < kPairRX = 33.  One warp per halo row (hy, hz)
-        // takes k < 32; the rows' last cells (k = 32) go one per thread.
-        auto red_cell = [&](int hy, int hz, int k) {
+        // Red cells of the halo tile, one warp per halo row (hy, hz): halo
+        // x = x0 - 1 + hx, hx = 2k + ((y + z + 1) & 1); lanes take k < 32 and
+        // the rows' last cells (k = 32) go one per thread afterwards.
+        auto red_row = [&](int hy, int hz, int k) {
             const int y = y0 - 1 + hy, z = z0 - 1 + hz;
             const int x = x0 - 1 + 2 * k + ((y + z + 1) & 1);
             float v = 0.0f;
-            if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && z >= 0 && z < L.nz) {
-                const long long ro = (long long)L.nx * y + nxy * z;
-                const float* row_e = ein + ro;
-                const float* ym = y > 0 ? row_e - L.nx : row_e;
-                const float* yp = y < L.ny - 1 ? row_e + L.nx : row_e;
-                const float* zm = z > 0 ? row_e - nxy : row_e;
-                const float* zp = z < L.nz - 1 ? row_e + nxy : row_e;
-                const int xm = x > 0 ? x - 1 : x, xp = x < L.nx - 1 ? x + 1 : x;
-                v = mg_relax(L, row_e[xm] + row_e[xp], ym[x] + yp[x], zm[x] + zp[x], r[ro + x], inv, row_e[x]);
+            if ((unsigned)x < (unsigned)nx && (unsigned)y < (unsigned)ny && (unsigned)z < (unsigned)nz) {
+                const int i = x + nx * y + nxy * z;
+                const int oym = y > 0 ? -nx : 0, oyp = y < ny - 1 ? nx : 0;
+                const int ozm = z > 0 ? -nxy : 0, ozp = z < nz - 1 ? nxy : 0;
+                const int oxm = x > 0 ? -1 : 0, oxp = x < nx - 1 ? 1 : 0;
+                const float* p = ein + i;
+                v = mg_relax(L, p[oxm] + p[oxp], p[oym] + p[oyp], p[ozm] + p[ozp], r[i], inv, p[0]);
             }
             red[hz][hy][k] = v;
         };
-        for (int row = tid >> 5; row < kPairHY * kPairHZ; row += 8) red_cell(row % kPairHY, row / kPairHY, tid & 31);
-        for (int row = tid; row < kPairHY * kPairHZ; row += 256) red_cell(row % kPairHY, row / kPairHY, kPairRX - 1);
+        for (int row = warp; row < kPairHY * kPairHZ; row += 8) red_row(row % kPairHY, row / kPairHY, lane);
+        for (int row = tid; row < kPairHY * kPairHZ; row += 256) red_row(row % kPairHY, row / kPairHY, kPairRX - 1);
         __syncthreads();
         // Output pairs: lane -> x = x0 + 2*lane + {0, 1}, warp -> y, loop over z.
-        const int lane = tid & 31, ty = tid >> 5;
-        const int y = y0 + ty, hy = ty + 1;
+        const int y = y0 + warp, hy = warp + 1;
         const int xa = x0 + 2 * lane;
-        if (y < L.ny && xa < L.nx) {
-            for (int tz = 0; tz < kPairTZ; ++tz) {
-                const int z = z0 + tz;
-                if (z >= L.nz) break;
-                const int hz = tz + 1;
-                const long long ro = (long long)L.nx * y + nxy * z;
-                // Of the pair, the red cell is xa + pr, the black one xa + 1 - pr.
+        if (y < ny && xa < nx) {
+            const int zend = min(kPairTZ, nz - z0);
+            int i0 = xa + nx * y + nxy * z0;
+            for (int tz = 0; tz < zend; ++tz, i0 += nxy) {
+                const int z = z0 + tz, hz = tz + 1;
+                // Of the pair, the red cell is xa + pr and the black one xa + 1 - pr.
                 const int pr = (xa + y + z) & 1;
                 const int xr = xa + pr, xb = xa + 1 - pr;
-                // Halo x index h = x - x0 + 1; red cell h >> 1 in its row.
-                if (xr < L.nx) eout[ro + xr] = red[hz][hy][(xr - x0 + 1) >> 1];
-                if (xb < L.nx) {
-                    const int h = xb - x0 + 1;
-                    const float c = ein[ro + xb];
-                    const float sx = (xb > 0 ? red[hz][hy][(h - 1) >> 1] : c) + (xb < L.nx - 1 ? red[hz][hy][(h + 1) >> 1] : c);
-                    const float sy = (y > 0 ? red[hz][hy - 1][h >> 1] : c) + (y < L.ny - 1 ? red[hz][hy + 1][h >> 1] : c);
-                    const float sz = (z > 0 ? red[hz - 1][hy][h >> 1] : c) + (z < L.nz - 1 ? red[hz + 1][hy][h >> 1] : c);
-                    eout[ro + xb] = mg_relax(L, sx, sy, sz, r[ro + xb], inv, c);
+                if (xr < nx) eout[i0 + pr] = red[hz][hy][(xr - x0 + 1) >> 1];
+                if (xb < nx) {
+                    const int h = (xb - x0 + 1) >> 1, hm = (xb - x0) >> 1, hp = (xb - x0 + 2) >> 1;
+                    const int ib = i0 + 1 - pr;
+                    const float c = ein[ib];
+                    const float sx = (xb > 0 ? red[hz][hy][hm] : c) + (xb < nx - 1 ? red[hz][hy][hp] : c);
+                    const float sy = (y > 0 ? red[hz][hy - 1][h] : c) + (y < ny - 1 ? red[hz][hy + 1][h] : c);
+                    const float sz = (z > 0 ? red[hz - 1][hy][h] : c) + (z < nz - 1 ? red[hz + 1][hy][h] : c);
+                    eout[ib] = mg_relax(L, sx, sy, sz, r[ib], inv, c);
                 }
             }
         }
