@@ -74,7 +74,11 @@ struct Ctl {
     unsigned int passes;
     unsigned int stopped;
     double last_div;               // dt/(rho h^2) * max|r| at the last check
+    unsigned int one;              // the next pass runs its first V-cycle only
 };
+
+// Whether the multigrid kernels of V-cycle vc (0 or 1 within a pass) skip a slot.
+__device__ __forceinline__ bool mg_off(const Ctl& c, int vc) { return c.stopped || (vc > 0 && c.one); }
 
 struct InstDev {
     Geom g;
@@ -312,6 +316,7 @@ __global__ void kb_init(const InstDev* inst, Ctl* ctl, int n) {
         ctl[s].maxr_bits = 0;
         ctl[s].passes = 0;
         ctl[s].stopped = inst[s].active ? 0u : 1u;
+        ctl[s].one = 0u;
         ctl[s].last_div = 0;
     }
 }
@@ -413,10 +418,20 @@ __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaG
         // binary64 round-off floor of the residual (|B| * 2^-53 and up):
         // stop there rather than spin to the pass cap.
         const bool stalled = count_pass && div > 0.9 * c.last_div;
+        const double prev = c.last_div;
         c.last_div = div;
         if (count_pass) c.passes += 1;
         const bool more =
             !gated(&st[s], gate) && div > I.thresh && !isinf(div) && !stalled && c.passes < I.max_refine;
+        // The last pass often needs one V-cycle, not two: from the reduction
+        // per V-cycle the pass just achieved, predict max|div| after one more
+        // V-cycle and run only that when it lands below half the threshold.
+        unsigned one = 0u;
+        if (count_pass && more && prev > 0.0) {
+            const double f = c.one ? div / prev : sqrt(div / prev);
+            one = (f < 1.0 && div * f <= 0.5 * I.thresh) ? 1u : 0u;
+        }
+        c.one = one;
         if (!more) c.stopped = 1;
         any |= more ? 1 : 0;
     }
@@ -465,9 +480,9 @@ __device__ __forceinline__ float mg_interp(float ax, float ay, float az, float e
 // space counts 32 lanes per row (row_box).
 __host__ __device__ inline long long row_box(const Lvl& L) { return 32ll * L.ny * L.nz; }
 
-__global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color) {
+__global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color, int vc) {
     FOR_TILES(tab)
-    if (ctl[s].stopped) continue;
+    if (mg_off(ctl[s], vc)) continue;
     const Lvl L = inst[s].lev[l];
     const long long rows = (long long)L.ny * L.nz;
     const long long nxy = (long long)L.nx * L.ny;
@@ -509,9 +524,9 @@ __device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) 
 
 // Coarse rhs = mean of the children's residuals; coarse solution = 0.  One
 // thread per coarse cell (row-wise forms of this kernel measured slower).
-__global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
+__global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
     FOR_TILES(tab)
-    if (ctl[s].stopped) continue;
+    if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
     const Lvl C = inst[s].lev[l + 1];
     const long long n = lvl_cells(C);
@@ -535,9 +550,9 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l)
 // axis the parent weighs 3/4 and the next coarse cell toward the fine cell
 // 1/4 (clamped at the walls, the Neumann reflection).  A warp owns one fine
 // (y, z) row (row_box of the fine level); its four coarse rows are fixed.
-__global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l) {
+__global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
     FOR_TILES(tab)
-    if (ctl[s].stopped) continue;
+    if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
     const Lvl C = inst[s].lev[l + 1];
     const long long rows = (long long)F.ny * F.nz;
@@ -600,12 +615,13 @@ __device__ float block_sum(float v, float* red) {
 constexpr int kPairTX = 64, kPairTY = 8, kPairTZ = 8;
 constexpr int kPairRX = kPairTX / 2 + 1, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
 
-__global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir) {
+__global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir,
+                                                      int vc) {
     __shared__ float red[kPairHZ][kPairHY][kPairRX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
-        if (ctl[s].stopped) continue;
+        if (mg_off(ctl[s], vc)) continue;
         const Lvl L = inst[s].lev[l];
         const float* __restrict__ ein = dir ? L.e2 : L.e;
         float* __restrict__ eout = dir ? L.e : L.e2;
@@ -698,12 +714,13 @@ __device__ __forceinline__ float sm_res(const Lvl& L, const float* e, const floa
     return mg_res(L, sx, sy, sz, c, r[i]);
 }
 
-__global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, const Ctl* ctl, Tab tab, int nu) {
+__global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, const Ctl* ctl, Tab tab, int nu,
+                                                           int vc) {
     extern __shared__ float tsm[];
     __shared__ float red[32];
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
-        if (ctl[s].stopped) continue;
+        if (mg_off(ctl[s], vc)) continue;
         const InstDev& I = inst[s];
         const int t = I.tail, nl = I.nlev;
         float* E[kMaxLev];
@@ -1091,43 +1108,46 @@ void enq_sweep(Batch* b, int axis, int parity, int phase, cudaStream_t s) {
     else LAUNCH(b, S_SWEEP, kb_sweep<2>, b->d_inst, b->d_st, t, parity, phase);
 }
 
-void enq_smooth(Batch* b, int st, int l, int pairs, cudaStream_t s) {
+void enq_smooth(Batch* b, int st, int l, int pairs, int vc, cudaStream_t s) {
     for (int k = 0; k < pairs; ++k) {
-        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 0);
-        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 1);
+        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 0, vc);
+        LAUNCH(b, st, kb_smooth, b->d_inst, b->d_ctl, tab(b, st), l, 1, vc);
     }
 }
 
 // Pre- or post-smoothing of level l: fused pairs ping-ponging through e2
 // (an even count returns the result to e) for slots that have e2, in-place
 // colour sweeps for the others.
-void enq_level_smooth(Batch* b, int l, cudaStream_t s) {
+void enq_level_smooth(Batch* b, int l, int vc, cudaStream_t s) {
     if (b->graph_pair & (1u << l))
         for (int k = 0; k < b->nu; ++k) {
-            kb_smooth_pair<<<grid(b, S_PAIR + l), 256, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1);
+            kb_smooth_pair<<<grid(b, S_PAIR + l), 256, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1, vc);
             ++b->launches;
         }
-    if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, s);
+    if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, vc, s);
 }
 
-void enq_vcycle(Batch* b, cudaStream_t s) {
+// V-cycle vc (0 or 1) of a refinement pass; slots whose pass runs one
+// V-cycle skip vc = 1.
+void enq_vcycle(Batch* b, int vc, cudaStream_t s) {
     const int L = b->graph_levels;
     for (int l = 0; l + 1 < L; ++l) {
-        enq_level_smooth(b, l, s);
-        LAUNCH(b, S_RESTRICT + l, kb_restrict, b->d_inst, b->d_ctl, tab(b, S_RESTRICT + l), l);
+        enq_level_smooth(b, l, vc, s);
+        LAUNCH(b, S_RESTRICT + l, kb_restrict, b->d_inst, b->d_ctl, tab(b, S_RESTRICT + l), l, vc);
     }
-    kb_vtail<<<grid(b, S_COARSE), kCoarseThreads, b->tail_smem, s>>>(b->d_inst, b->d_ctl, tab(b, S_COARSE), b->nu);
+    kb_vtail<<<grid(b, S_COARSE), kCoarseThreads, b->tail_smem, s>>>(b->d_inst, b->d_ctl, tab(b, S_COARSE), b->nu,
+                                                                      vc);
     ++b->launches;
     for (int l = 0; l < L; ++l)
-        if (b->graph_big & (1u << l)) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, s);
+        if (b->graph_big & (1u << l)) enq_smooth(b, S_BIGCOARSE + l, l, 8 * b->nu, vc, s);
     for (int l = L - 2; l >= 0; --l) {
-        LAUNCH(b, S_PROLONG + l, kb_prolong, b->d_inst, b->d_ctl, tab(b, S_PROLONG + l), l);
-        enq_level_smooth(b, l, s);
+        LAUNCH(b, S_PROLONG + l, kb_prolong, b->d_inst, b->d_ctl, tab(b, S_PROLONG + l), l, vc);
+        enq_level_smooth(b, l, vc, s);
     }
 }
 
 void enq_pass(Batch* b, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int gate) {
-    for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, s);
+    for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, k > 0 ? 1 : 0, s);
     LAUNCH(b, S_INT, kb_correct, b->d_inst, b->d_ctl, tab(b, S_INT));
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 1);
     kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate);
@@ -1812,11 +1832,11 @@ std::string batch_tune(Batch* b, int reps) {
         else if (st == S_INT) kb_residual<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, t, 0, 0);
         else if (st == S_PBC) kb_pbc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0);
         else if (st == S_GRAD) kb_grad<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
-        else if (st >= S_SMOOTH && st < S_RESTRICT) kb_smooth<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_SMOOTH, 0);
+        else if (st >= S_SMOOTH && st < S_RESTRICT) kb_smooth<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_SMOOTH, 0, 0);
         else if (st >= S_RESTRICT && st < S_PROLONG)
-            kb_restrict<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_RESTRICT);
+            kb_restrict<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_RESTRICT, 0);
         else if (st >= S_PROLONG && st < S_BIGCOARSE)
-            kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG);
+            kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG, 0);
     };
     std::vector<int> stages = {S_BC, S_SHADOW, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD};
     for (int l = 0; l + 1 < L; ++l) {
