@@ -93,6 +93,7 @@ SIGNATURES = {
     "af_phase_pressure_bc": (C.c_int, [_E]),
     "af_phase_subtract_gradient": (C.c_int, [_E]),
     "af_last_projection_stats": (C.c_int, [_E, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "af_last_projection_vcycles": (C.c_int, [_E, C.POINTER(C.c_int64)]),
     "af_profile": (C.c_int, [_E, C.c_int]),
     "af_last_step_profile": (C.c_int, [_E, C.POINTER(AfStepProfile)]),
     "af_device_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),

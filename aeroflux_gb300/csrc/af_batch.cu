@@ -74,11 +74,13 @@ struct Ctl {
     unsigned int passes;
     unsigned int stopped;
     double last_div;               // dt/(rho h^2) * max|r| at the last check
-    unsigned int one;              // the next pass runs its first V-cycle only
+    unsigned int nv;               // V-cycles the next pass runs (0: all of them)
+    double vfac;                   // measured max|div| reduction per V-cycle (0: none yet); kept across projections
+    unsigned int vtotal;           // V-cycles the current projection has run
 };
 
-// Whether the multigrid kernels of V-cycle vc (0 or 1 within a pass) skip a slot.
-__device__ __forceinline__ bool mg_off(const Ctl& c, int vc) { return c.stopped || (vc > 0 && c.one); }
+// Whether the multigrid kernels of V-cycle vc of a pass skip a slot.
+__device__ __forceinline__ bool mg_off(const Ctl& c, int vc) { return c.stopped || (c.nv && (unsigned)vc >= c.nv); }
 
 struct InstDev {
     Geom g;
@@ -316,7 +318,8 @@ __global__ void kb_init(const InstDev* inst, Ctl* ctl, int n) {
         ctl[s].maxr_bits = 0;
         ctl[s].passes = 0;
         ctl[s].stopped = inst[s].active ? 0u : 1u;
-        ctl[s].one = 0u;
+        ctl[s].nv = 0u;
+        ctl[s].vtotal = 0u;
         ctl[s].last_div = 0;
     }
 }
@@ -404,7 +407,7 @@ __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
 // One block: per slot, whether another refinement pass runs; the WHILE
 // condition is "any slot continues".  Bounded by each slot's max_refine.
 __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaGraphConditionalHandle h, int use_cond,
-                         int count_pass, int gate) {
+                         int count_pass, int gate, int vcycles) {
     int any = 0;
     for (int s = threadIdx.x; s < n; s += blockDim.x) {
         const InstDev& I = inst[s];
@@ -423,15 +426,23 @@ __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaG
         if (count_pass) c.passes += 1;
         const bool more =
             !gated(&st[s], gate) && div > I.thresh && !isinf(div) && !stalled && c.passes < I.max_refine;
-        // The last pass often needs one V-cycle, not two: from the reduction
-        // per V-cycle the pass just achieved, predict max|div| after one more
-        // V-cycle and run only that when it lands below half the threshold.
-        unsigned one = 0u;
-        if (count_pass && more && prev > 0.0) {
-            const double f = c.one ? div / prev : sqrt(div / prev);
-            one = (f < 1.0 && div * f <= 0.5 * I.thresh) ? 1u : 0u;
+        // The last pass often needs fewer V-cycles than the others: from the
+        // reduction per V-cycle the pass just achieved, predict how many more
+        // bring max|div| below half the threshold, and run only those.
+        // The first pass of a projection uses the factor the slot's last
+        // projection measured.
+        if (count_pass) c.vtotal += c.nv ? c.nv : (unsigned)vcycles;
+        if (count_pass && prev > 0.0) {
+            const double ran = c.nv ? (double)c.nv : (double)vcycles;
+            const double f = pow(div / prev, 1.0 / ran);
+            if (f < 1.0) c.vfac = f;
         }
-        c.one = one;
+        unsigned nv = 0u;
+        if (more && c.vfac > 0.0 && c.vfac < 1.0) {
+            const double k = ceil(log(0.5 * I.thresh / div) / log(c.vfac));
+            if (k >= 1.0 && k < (double)vcycles) nv = (unsigned)k;
+        }
+        c.nv = nv;
         if (!more) c.stopped = 1;
         any |= more ? 1 : 0;
     }
@@ -966,7 +977,7 @@ struct Batch {
     cudaEvent_t ev[kNumEvents] = {};
     int64_t launches = 0;
     int nu = 2;
-    int vcycles = 2;
+    int vcycles = 4;  // V-cycles per refinement pass at most (measured best of 2, 3, 4, 6, 8)
     int fixed_passes = 0;
     cudaError_t capture_err = cudaSuccess;
 };
@@ -1127,8 +1138,8 @@ void enq_level_smooth(Batch* b, int l, int vc, cudaStream_t s) {
     if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, vc, s);
 }
 
-// V-cycle vc (0 or 1) of a refinement pass; slots whose pass runs one
-// V-cycle skip vc = 1.
+// V-cycle vc of a refinement pass; slots whose pass runs fewer V-cycles
+// skip it.
 void enq_vcycle(Batch* b, int vc, cudaStream_t s) {
     const int L = b->graph_levels;
     for (int l = 0; l + 1 < L; ++l) {
@@ -1147,10 +1158,10 @@ void enq_vcycle(Batch* b, int vc, cudaStream_t s) {
 }
 
 void enq_pass(Batch* b, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int gate) {
-    for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, k > 0 ? 1 : 0, s);
+    for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, k, s);
     LAUNCH(b, S_INT, kb_correct, b->d_inst, b->d_ctl, tab(b, S_INT));
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 1);
-    kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate);
+    kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate, b->vcycles);
     ++b->launches;
 }
 
@@ -1163,7 +1174,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
     ++b->launches;
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 0);
     if (b->fixed_passes > 0) {
-        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, 0, 0, 0, gate);
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, 0, 0, 0, gate, b->vcycles);
         ++b->launches;
         for (int k = 0; k < b->fixed_passes; ++k) enq_pass(b, s, 0, 0, gate);
     } else {
@@ -1181,7 +1192,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
             b->capture_err = rc;
             return;
         }
-        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, 1, 0, gate);
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, 1, 0, gate, b->vcycles);
         ++b->launches;
         if ((rc = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps)) != cudaSuccess) {
             b->capture_err = rc;
@@ -1313,6 +1324,7 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     // projection's pressure instead of zero (project.go:81-83 zeroes it for
     // the fixed sweep count of the red-black solver).
     if (const char* cs = getenv("AEROFLUX_COLD_START")) b->cold = atoi(cs) != 0;
+    if (const char* vc = getenv("AEROFLUX_MG_VCYCLES")) b->vcycles = std::min(8, std::max(1, atoi(vc)));
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{256, 1, 8};
@@ -1560,6 +1572,7 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.max_refine = (unsigned)c.max_refine;
     I.parity = 0;
     I.warm = b->cold ? 0 : 1;
+    cudaMemsetAsync(b->d_ctl + s, 0, sizeof(Ctl), b->stream);  // no measured V-cycle factor yet
     // Smoothing sweeps per level are a property of the batch's step graph:
     // the first slot of an empty batch sets them.
     b->nu = batch_nu;
@@ -1762,12 +1775,13 @@ bool batch_slot_faulted(const Batch* b, int s, std::string* msg) {
     return true;
 }
 
-void batch_slot_projection(Batch* b, int s, int64_t* passes, double* max_div) {
+void batch_slot_projection(Batch* b, int s, int64_t* passes, double* max_div, int64_t* vcycles) {
     Ctl c;
     cudaStreamSynchronize(b->stream);
     cudaMemcpy(&c, b->d_ctl + s, sizeof c, cudaMemcpyDeviceToHost);
     *passes = c.passes;
     *max_div = c.last_div;
+    if (vcycles) *vcycles = c.vtotal;
 }
 
 cudaError_t batch_profile(Batch* b, bool on) {

@@ -64,7 +64,9 @@ cudaError_t batch_seed(Batch* b, int slot, double amp, double noise, uint64_t se
 // slots that faulted in it; `msg` gets the first faulting slot's message.
 int batch_collect_faults(Batch* b, std::string* msg, int* first_slot);
 bool batch_slot_faulted(const Batch* b, int slot, std::string* msg);
-void batch_slot_projection(Batch* b, int slot, int64_t* passes, double* max_div);
+// Refinement passes, estimated max|div| and multigrid V-cycles of the slot's
+// last projection.
+void batch_slot_projection(Batch* b, int slot, int64_t* passes, double* max_div, int64_t* vcycles = nullptr);
 
 // Times the candidate launch shapes of every stage on the current slots and
 // keeps the fastest; returns a JSON report.  Results do not depend on it.

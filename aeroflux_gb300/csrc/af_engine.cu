@@ -887,6 +887,19 @@ int af_set_advection(af_engine* e, int scheme) {
     return AF_OK;
 }
 
+int af_last_projection_vcycles(af_engine* e, int64_t* vcycles) {
+    if (int rc = check_open(e)) return rc;
+    if (!vcycles) return AF_ERR_ARG;
+    *vcycles = 0;
+    af::Batch* b = e->mg ? e->mg : e->batch;
+    if (!b) return AF_OK;
+    AF_CUDA(e, cudaStreamSynchronize(e->stream));
+    int64_t passes = 0;
+    double md = 0;
+    af::batch_slot_projection(b, 0, &passes, &md, vcycles);
+    return AF_OK;
+}
+
 int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div) {
     if (int rc = check_open(e)) return rc;
     if (!passes || !max_div) return AF_ERR_ARG;

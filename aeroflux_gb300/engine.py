@@ -289,6 +289,11 @@ class Engine:
         self._check(L.lib().af_last_projection_stats(self._h, C.byref(passes), C.byref(md)))
         return passes.value, md.value
 
+    def LastProjectionVCycles(self) -> int:
+        v = C.c_int64()
+        self._check(L.lib().af_last_projection_vcycles(self._h, C.byref(v)))
+        return v.value
+
     def SeedDevice(self, amp: float = 1.0, noise: float = 0.01, seed: int = 42, stream: int = 0) -> None:
         """Device-side Taylor-Green + PCG32 initial field (apply the BC after)."""
         self._device_op(L.lib().af_seed_device, amp, noise, seed, stream)

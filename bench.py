@@ -213,18 +213,18 @@ def bench_reference(args):
     return 0
 
 
-def mixed_bytes_per_cell_step(passes: float, nu: int = 2, vcycles: int = 2) -> float:
+def mixed_bytes_per_cell_step(passes: float, vcycles: float, nu: int = 2) -> float:
     """Algorithmic bytes per cell-step of the mixed form at its stored widths
-    (binary64 state, binary32 multigrid): six sweeps (read U, V, W, write
-    three faces: 48 B); per projection the divergence (read U, V, W, write
-    Div: 32 B), the first residual (read p, B, write r, zero e: 24 B), per
-    refinement pass the correction (read p, e, write p: 20 B), the residual
-    (24 B) and the V-cycles (per level cell: 2*nu fused red-black pairs of
-    12 B, restriction 9 B, prolongation 8.5 B; the coarser levels add 1/7),
-    and the gradient (read p, read and write U, V, W: 56 B)."""
+    (binary64 state, binary32 multigrid), for a projection of `passes`
+    refinement passes and `vcycles` V-cycles in all: six sweeps (read U, V,
+    W, write three faces: 48 B); per projection the divergence (read U, V,
+    W, write Div: 32 B), the first residual (read p, B, write r, zero e:
+    24 B), per pass the correction (read p, e, write p: 20 B) and the
+    residual (24 B), per V-cycle (per level cell) 2*nu fused red-black pairs
+    of 12 B, restriction 9 B and prolongation 8.5 B, the coarser levels
+    adding 1/7, and the gradient (read p, read and write U, V, W: 56 B)."""
     vcycle = (2 * nu * 12 + 9 + 8.5) * 8 / 7
-    per_pass = 20 + 24 + vcycles * vcycle
-    return 6 * 48 + 2 * (32 + 24 + passes * per_pass + 56)
+    return 6 * 48 + 2 * (32 + 24 + passes * 44 + vcycles * vcycle + 56)
 
 
 def new_engine(precision: int, local: int, rank: int, div_tol: float = 0.0):
@@ -250,7 +250,7 @@ def device_timed(e, steps: int, warmup: int, dist, clocks=None):
         clocks.start()
         time.sleep(0.3)
     dev_ms = solve_ms = sw_ms = 0.0
-    passes = []
+    passes, vcyc = [], []
     t0 = time.perf_counter()
     prof = None
     for _ in range(steps):
@@ -260,12 +260,14 @@ def device_timed(e, steps: int, warmup: int, dist, clocks=None):
         solve_ms += prof.rbgs_ms
         sw_ms += prof.sweep_ms
         passes.append(e.LastProjectionStats()[0])
+        vcyc.append(e.LastProjectionVCycles())
     wall = time.perf_counter() - t0
     clk = clocks.stop() if clocks else None
     dist.barrier()
     e.Profile(False)
     return {"dev_s": dist.max(dev_ms / 1e3), "wall_s": wall, "solve_ms": solve_ms / steps, "sweep_ms": sw_ms / steps,
-            "launches": prof.kernel_launches, "rbgs_launches": prof.rbgs_launches, "passes": passes, "clocks": clk}
+            "launches": prof.kernel_launches, "rbgs_launches": prof.rbgs_launches, "passes": passes, "vcycles": vcyc,
+            "clocks": clk}
 
 
 def bench_mixed_512(args, dist, local, rank):
@@ -432,10 +434,12 @@ def bench_ours(args):
         em, _ = new_engine(L.AF_PRECISION_MIXED, local, rank, tol)
         tm = device_timed(em, args.steps, args.warmup, dist)
         mv = cells * args.steps * world / tm["dev_s"]
-        mb = mixed_bytes_per_cell_step(statistics.mean(tm["passes"]))
+        # Both projections of a step counted as the last one (passes and V-cycles).
+        mb = mixed_bytes_per_cell_step(statistics.mean(tm["passes"]), statistics.mean(tm["vcycles"]))
         mixed[label] = {"value": mv, "unit": UNIT, "ms_per_step": tm["dev_s"] * 1e3 / args.steps,
                         "div_tol": tol, "max_divergence_after": em.MaxDivergence(),
                         "refinement_passes_last_projection": tm["passes"],
+                        "vcycles_last_projection": tm["vcycles"],
                         "stages_ms_per_step": {"projections": tm["solve_ms"], "sweeps": tm["sweep_ms"]},
                         "speedup_vs_plain": mv / value,
                         "roofline": {"bound": "hbm", "scope": "whole step", "algorithmic_bytes_per_cell_step": mb,

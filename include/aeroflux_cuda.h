@@ -198,6 +198,10 @@ int af_phase_subtract_gradient(af_engine* e);
 /* Statistics of the last projection of a MIXED engine: refinement passes
  * and the FP64 max|div| reached.  FP64 engines report 0 passes. */
 int af_last_projection_stats(af_engine* e, int64_t* passes, double* max_div);
+/* Multigrid V-cycles the last refined projection ran in total (its passes
+ * run up to four each, fewer when the measured reduction predicts them
+ * enough); 0 for the red-black form. */
+int af_last_projection_vcycles(af_engine* e, int64_t* vcycles);
 
 /* Device-time profile of the last Step, from event nodes the step graph
  * carries while profiling is on (af_profile).  No counterpart in the
