@@ -132,14 +132,19 @@ struct Tab {
     int ept;
 };
 
+// Every lane of a warp asks for the same item (callers are block-uniform
+// and blocks are whole warps): lane 0 searches, the warp shares the result.
 __device__ __forceinline__ int find_slot(const int* prefix, int n, int item) {
-    int lo = 0, hi = n;  // prefix[lo] <= item < prefix[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= item) lo = mid;
-        else hi = mid;
+    int lo = 0;
+    if ((threadIdx.x & 31) == 0) {
+        int hi = n;  // prefix[lo] <= item < prefix[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (prefix[mid] <= item) lo = mid;
+            else hi = mid;
+        }
     }
-    return lo;
+    return __shfl_sync(0xffffffffu, lo, 0);
 }
 
 // Loop over this block's tiles; `s` is the slot, `first` the first element
