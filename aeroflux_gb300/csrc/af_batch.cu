@@ -110,8 +110,8 @@ struct InstDev {
 
 // Stage ids.  Level stages take kMaxLev consecutive ids.
 enum {
-    S_BC = 0, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD, S_COARSE, S_SHADOW,
-    S_SMOOTH = 8,
+    S_BC = 0, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD, S_COARSE, S_SHADOW, S_CORR,
+    S_SMOOTH = 9,
     S_RESTRICT = S_SMOOTH + kMaxLev,
     S_PROLONG = S_RESTRICT + kMaxLev,
     S_BIGCOARSE = S_PROLONG + kMaxLev,
@@ -239,44 +239,53 @@ __global__ void kb_pbc(const InstDev* inst, Status* st, Tab tab, int gate) {
     END_TILES
 }
 
-__device__ __forceinline__ bool face_of(const InstDev& I, long long el, int* c, int* x, int* y, int* z) {
-    const Geom& g = I.g;
-    const unsigned e = (unsigned)el, r = I.ffx.div(e), r2 = I.ffy.div(r), cc = I.ffz.div(r2);
-    *x = g.G + (int)(e - r * (unsigned)(g.NX + 1));
-    *y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1));
-    *z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
-    *c = (int)cc;
-    return *x < g.G + g.NX + (*c == 0) && *y < g.G + g.NY + (*c == 1) && *z < g.G + g.NZ + (*c == 2);
-}
-
+// subtractGradient over every face, a warp per (component, y, z) face row.
 __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, int gate) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (gated(&st[s], gate)) continue;
-    const long long n = face_box(I.g);
+    const Geom& g = I.g;
+    const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1);
+    double* u = cur(I, 1, parity);
+    double* v = cur(I, 2, parity);
+    double* w = cur(I, 3, parity);
     FOR_ELEMS(tab)
-    if (el >= n) break;
-    int c, x, y, z;
-    if (face_of(I, el, &c, &x, &y, &z))
-        grad_face(I.g, I.slot[0], cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.grad_scale, c, x, y, z);
+    const long long row = el >> 5;
+    if (row >= rows) break;
+    const int lane = (int)(el & 31);
+    const unsigned r = (unsigned)row, r2 = I.ffy.div(r), cc = I.ffz.div(r2);
+    const int c = (int)cc;
+    const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
+    if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
+    const int x1 = g.G + g.NX + (c == 0);
+    for (int x = g.G + lane; x < x1; x += 32) grad_face(g, I.slot[0], u, v, w, I.grad_scale, c, x, y, z);
     END_ELEMS
     END_TILES
 }
 
 // binary32 shadow of the current U, V, W (every element, ghosts included),
-// converted once per sweep instead of once per tap.
+// converted once per sweep instead of once per tap.  A thread converts four
+// consecutive elements of one field (two 16-byte loads, one 16-byte store;
+// fields start on 128-byte boundaries); the iteration space counts quads.
+__host__ __device__ inline long long quads(long long n) { return (n + 3) / 4; }
+
 __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
-    const long long nu = I.g.u.count, nv = I.g.v.count, n = nu + nv + I.g.w.count;
-    const double* u = cur(I, 1, parity);
-    const double* v = cur(I, 2, parity);
-    const double* w = cur(I, 3, parity);
+    const long long qu = quads(I.g.u.count), qv = quads(I.g.v.count), n = qu + qv + quads(I.g.w.count);
     FOR_ELEMS(tab)
     if (el >= n) break;
-    if (el < nu) I.sh[0][el] = f64_to_f32(u[el]);
-    else if (el < nu + nv) I.sh[1][el - nu] = f64_to_f32(v[el - nu]);
-    else I.sh[2][el - nu - nv] = f64_to_f32(w[el - nu - nv]);
+    const int f = el < qu ? 0 : (el < qu + qv ? 1 : 2);
+    const long long q = el - (f == 0 ? 0 : (f == 1 ? qu : qu + qv));
+    const long long count = f == 0 ? I.g.u.count : (f == 1 ? I.g.v.count : I.g.w.count);
+    const double* src = cur(I, 1 + f, parity) + 4 * q;
+    float* dst = I.sh[f] + 4 * q;
+    if (4 * q + 4 <= count) {
+        const double2 a = reinterpret_cast<const double2*>(src)[0], b = reinterpret_cast<const double2*>(src)[1];
+        reinterpret_cast<float4*>(dst)[0] = make_float4(f64_to_f32(a.x), f64_to_f32(a.y), f64_to_f32(b.x), f64_to_f32(b.y));
+    } else {
+        for (long long k = 0; 4 * q + k < count; ++k) dst[k] = f64_to_f32(src[k]);
+    }
     END_ELEMS
     END_TILES
 }
@@ -393,18 +402,22 @@ __global__ void kb_residual(const InstDev* inst, Status* st, Ctl* ctl, Tab tab, 
     if (held >= 0) warp_max_commit(m, &ctl[held].maxr_bits);
 }
 
+// p += e over the interior, a warp per (y, z) row (32 lanes per row).
 __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (ctl[s].stopped) continue;
     const Geom& g = I.g;
-    const long long n = (long long)g.NX * g.NY * g.NZ;
+    const long long rows = (long long)g.NY * g.NZ;
     FOR_ELEMS(tab)
-    if (el >= n) break;
-    const unsigned e = (unsigned)el, r2 = I.fnx.div(e), zz = I.fny.div(r2);
-    const long long i = (g.G + (int)(e - r2 * (unsigned)g.NX)) + (g.G + (int)(r2 - zz * (unsigned)g.NY)) * g.p.sy +
-                        (g.G + (int)zz) * g.p.sz;
-    I.slot[0][i] += f32_to_f64(I.lev[0].e[el]);
+    const long long row = el >> 5;
+    if (row >= rows) break;
+    const int lane = (int)(el & 31);
+    const unsigned zz = I.fny.div((unsigned)row);
+    const int y = (int)((unsigned)row - zz * (unsigned)g.NY), z = (int)zz;
+    double* p = I.slot[0] + g.G + (long long)(g.G + y) * g.p.sy + (long long)(g.G + z) * g.p.sz;
+    const float* e = I.lev[0].e + (long long)g.NX * y + (long long)g.NX * g.NY * z;
+    for (int x = lane; x < g.NX; x += 32) p[x] += f32_to_f64(e[x]);
     END_ELEMS
     END_TILES
 }
@@ -1031,11 +1044,11 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     const long long per = (long long)sh.tpb * sh.ept;
     long long n = 0;
     if (st == S_BC) n = bc_count(I.g);
-    else if (st == S_SWEEP) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
-    else if (st == S_GRAD) n = face_box(I.g);
-    else if (st == S_SHADOW) n = I.g.u.count + I.g.v.count + I.g.w.count;
+    else if (st == S_SWEEP || st == S_GRAD) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
+    else if (st == S_SHADOW) n = quads(I.g.u.count) + quads(I.g.v.count) + quads(I.g.w.count);
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
+    else if (st == S_CORR) n = 32ll * I.g.NY * I.g.NZ;
     else if (st == S_PBC) n = pbc_count(I.g);
     else if (st == S_COARSE) return I.tail >= 0 ? 1 : 0;
     const int lim = I.tail >= 0 ? I.tail : I.nlev - 1;  // levels smoothed by per-level kernels
@@ -1164,7 +1177,7 @@ void enq_vcycle(Batch* b, int vc, cudaStream_t s) {
 
 void enq_pass(Batch* b, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int gate) {
     for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, k, s);
-    LAUNCH(b, S_INT, kb_correct, b->d_inst, b->d_ctl, tab(b, S_INT));
+    LAUNCH(b, S_CORR, kb_correct, b->d_inst, b->d_ctl, tab(b, S_CORR));
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 1);
     kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate, b->vcycles);
     ++b->launches;
