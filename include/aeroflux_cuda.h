@@ -79,7 +79,8 @@ typedef struct af_config {
     int32_t precision;           /* af_precision */
     int32_t device;              /* CUDA device ordinal the engine lives on */
     double div_tol;              /* MIXED: stop refining once max|div| <= div_tol (0: 1e-10) */
-    int64_t inner_sweeps;        /* MIXED: binary32 smoothing sweeps per level (0: default) */
+    int64_t inner_sweeps;        /* MIXED: red-black smoothing pairs per level before and after
+                                    each coarse correction (0: 2) */
     int64_t max_refine;          /* MIXED: cap on refinement passes per projection (0: 30) */
 } af_config;
 

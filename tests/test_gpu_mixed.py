@@ -51,6 +51,16 @@ def test_projection_reaches_tolerance(n):
     e.Close()
 
 
+def test_projection_reports_its_vcycles():
+    e = seeded(mixed_cfg((48, 32, 96)))
+    e.project()
+    passes, _ = e.LastProjectionStats()
+    vc = e.LastProjectionVCycles()
+    # Up to four V-cycles per refinement pass, at least one.
+    assert passes <= vc <= 4 * passes
+    e.Close()
+
+
 @pytest.mark.parametrize("sweeps", [1, 3, 4])
 def test_projection_reaches_tolerance_with_any_sweep_count(sweeps):
     # Odd counts smooth in place, even counts with fused red-black pairs.
