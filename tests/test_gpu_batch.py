@@ -177,4 +177,12 @@ def test_benchmark_batch_reaches_tolerance():
     for s in (0, 17, 255):
         ref = alone(cfgs[s], s, 2)
         assert np.array_equal(bits(b.download(s, "U")), bits(ref["U"]))
+    # The benchmark configuration's full 300 Steps: every grid stays finite
+    # and divergence-free to the tolerance.
+    b.step(298)
+    worst = max(b.max_divergence(s) for s in slots)
+    print(f"256 uneven grids, 300 steps: worst max|div| {worst:.3e}")
+    assert worst <= 1e-10
+    for s in (3, 101, 200):
+        assert np.all(np.isfinite(b.download(s, "U")))
     b.close()

@@ -168,3 +168,26 @@ def test_mixed_256_cube_reaches_1e10_every_step():
     for name in ("U", "V", "W", "P"):
         assert np.all(np.isfinite(e.download(name)))
     e.Close()
+
+
+@pytest.mark.slow
+def test_c3_512_cube_100_steps_every_projection_reaches_1e10():
+    # The mixed-precision benchmark configuration at its full size and step
+    # count: 512^3, DT=0.0005, nu=1e-5, Taylor-Green + 0.05 noise, 100 Steps.
+    from aeroflux_gb300.workloads import MIXED_512
+    e = New(MIXED_512.config())
+    e.SeedDevice(1.0, MIXED_512.noise, 42, 0)
+    e.applyVelocityBC()
+    worst, passes = 0.0, []
+    for _ in range(MIXED_512.steps):
+        e.Step(1)
+        p, est = e.LastProjectionStats()
+        passes.append(p)
+        worst = max(worst, est)
+    md = e.MaxDivergence()
+    ke = e.KineticEnergy()
+    print(f"512^3 x 100 steps: max|div| {md:.3e}, worst estimate {worst:.3e}, passes {min(passes)}-{max(passes)}, "
+          f"KE {ke:.6e}")
+    assert md <= 1e-10 and worst <= 1e-10
+    assert math.isfinite(ke) and 0 < ke
+    e.Close()
