@@ -179,7 +179,6 @@ __host__ __device__ inline long long face_box(const Geom& g) {
 __host__ __device__ inline long long pbc_count(const Geom& g) {
     return 2ll * g.NY * g.NZ + 2ll * (g.NX + 2) * g.NZ + 2ll * (g.NX + 2) * (g.NY + 2);
 }
-__host__ __device__ inline long long half_box(const Lvl& L) { return (long long)((L.nx + 1) / 2) * L.ny * L.nz; }
 __host__ __device__ inline long long lvl_cells(const Lvl& L) { return (long long)L.nx * L.ny * L.nz; }
 
 // --- binary64 stages (bit-identical to the FP64 form's cells) -------------
@@ -945,11 +944,6 @@ struct Pool {
         }
         free_[off] = bytes;
     }
-    size_t free_bytes() const {
-        size_t f = 0;
-        for (auto& kv : free_) f += kv.second;
-        return f;
-    }
 };
 
 struct SlotHost {
@@ -1216,7 +1210,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
             b->capture_err = rc;
             return;
         }
-        cudaGraphNodeParams params{cudaGraphNodeTypeConditional};
+        cudaGraphNodeParams params{cudaGraphNodeTypeConditional};  // the other members value-initialised
         params.conditional.handle = h;
         params.conditional.type = cudaGraphCondTypeWhile;
         params.conditional.size = 1;
@@ -1402,7 +1396,7 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
     while (true) {
         Lvl& L = lev[n++];
         L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr,
-                FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2))};
+                FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr};
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
         if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;

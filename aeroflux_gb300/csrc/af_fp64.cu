@@ -831,7 +831,7 @@ extern "C" int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, 
         return AF_ERR_ARG;
     }
     if (cfg->nz > kNoAllocMaxPlanes || cfg->nx >= (1 << 20) || cfg->ny >= (1 << 20)) {
-        char m[160];
+        char m[256];
         snprintf(m, sizeof m,
                  "aeroflux: kinetic energy without allocation supports at most %d z-planes (and nx, ny < 2^20), "
                  "got %lldx%lldx%lld",
