@@ -38,7 +38,8 @@ def seeded(cfg, noise=0.01):
     return e
 
 
-@pytest.mark.parametrize("n", [(16, 16, 16), (32, 32, 32), (24, 20, 18), (33, 17, 20), (48, 32, 96)])
+@pytest.mark.parametrize("n", [(16, 16, 16), (32, 32, 32), (24, 20, 18), (33, 17, 20), (48, 32, 96), (1, 1, 1),
+                               (40, 1, 1), (3, 2, 5)])
 def test_projection_reaches_tolerance(n):
     e = seeded(mixed_cfg(n))
     before = e.MaxDivergence()
@@ -47,7 +48,7 @@ def test_projection_reaches_tolerance(n):
     md = e.MaxDivergence()
     print(f"{n}: max|div| {before:.3e} -> {md:.3e} in {passes} passes (estimate {est:.3e})")
     assert md <= 1e-10
-    assert 1 <= passes <= e.Cfg.MaxRefine
+    assert 0 <= passes <= e.Cfg.MaxRefine  # 0: the field needed no correction
     e.Close()
 
 

@@ -25,6 +25,8 @@ SHAPES = {
     "odd10x7x5": (dict(NX=10, NY=7, NZ=5, H=0.1, DT=0.003, Viscosity=1e-3, GaussSeidelIters=12), "tg", 1.0),
     "ghost2": (dict(NX=9, NY=6, NZ=11, Ghost=2, H=1 / 11, DT=0.004, Viscosity=5e-4, GaussSeidelIters=10), "tg", 1.0),
     "thin1x3x2": (dict(NX=1, NY=3, NZ=2, H=0.5, DT=0.01, GaussSeidelIters=3), "tg", 1.0),
+    "cell1x1x1": (dict(NX=1, NY=1, NZ=1, H=1.0, DT=0.01, GaussSeidelIters=2), "tg", 1.0),
+    "line40x1x1": (dict(NX=40, NY=1, NZ=1, H=1 / 40, DT=0.002, Viscosity=1e-3, GaussSeidelIters=5), "tg", 1.0),
     "cfl4": (dict(NX=16, NY=12, NZ=10, H=1 / 16, DT=0.01, Viscosity=1e-5, GaussSeidelIters=6), "tg", 25.0),
     "rect33x17x20": (dict(NX=33, NY=17, NZ=20, H=1 / 33, DT=0.002, Viscosity=1e-5, GaussSeidelIters=8), "tg", 1.0),
 }
