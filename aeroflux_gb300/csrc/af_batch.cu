@@ -67,6 +67,7 @@ struct Lvl {
     float* r;
     FastDiv fnx, fny, fhx;  // nx, ny, (nx+1)/2
     float* e2;              // second buffer of the fused red-black pair (levels below the tail)
+    FastDiv ftx, fty;       // fused-pair tiles along x and y
 };
 
 struct Ctl {
@@ -655,12 +656,9 @@ __global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const
         float* __restrict__ eout = dir ? L.e : L.e2;
         const float* __restrict__ r = L.r;
         const int nx = L.nx, ny = L.ny, nz = L.nz, nxy = nx * ny;  // a level holds < 2^31 cells
-        const int ntx = (nx + kPairTX - 1) / kPairTX, nty = (ny + kPairTY - 1) / kPairTY;
-        int local = item - tab.prefix[s];
-        const int bx = local % ntx;
-        local /= ntx;
-        const int by = local % nty;
-        const int bz = local / nty;
+        const unsigned local = (unsigned)(item - tab.prefix[s]);
+        const unsigned q1 = L.ftx.div(local), q2 = L.fty.div(q1);
+        const int bx = (int)(local - q1 * L.ftx.d), by = (int)(q1 - q2 * L.fty.d), bz = (int)q2;
         const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairTZ;
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
         // Red cells of the halo tile, one warp per halo row (hy, hz): halo
@@ -1396,7 +1394,8 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
     while (true) {
         Lvl& L = lev[n++];
         L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr,
-                FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr};
+                FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr,
+                FastDiv((unsigned)((nx + kPairTX - 1) / kPairTX)), FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY))};
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
         if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;
