@@ -561,14 +561,53 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l,
     const long long n = lvl_cells(C);
     const int ex = F.cx ? 2 : 1, ey = F.cy ? 2 : 1, ez = F.cz ? 2 : 1;
     const float inv = 1.0f / (float)(ex * ey * ez);
+    const bool full = ex == 2 && ey == 2 && ez == 2;
+    const long long nxy = (long long)F.nx * F.ny;
     FOR_ELEMS(tab)
     if (el >= n) break;
     const unsigned e = (unsigned)el, r = C.fnx.div(e), zz = C.fny.div(r);
     const int X = (int)(e - r * (unsigned)C.nx), Y = (int)(r - zz * (unsigned)C.ny), Z = (int)zz;
     float sum = 0.0f;
-    for (int dz = 0; dz < ez; ++dz)
-        for (int dy = 0; dy < ey; ++dy)
-            for (int dx = 0; dx < ex; ++dx) sum += mg_residual(F, X * ex + dx, Y * ey + dy, Z * ez + dz);
+    if (full) {
+        // The 2x2x2 children and their 24 face neighbours, each loaded once
+        // (a neighbour across a wall is the child itself); then the eight
+        // residuals of mg_residual in the same order.
+        const int x0 = 2 * X, y0 = 2 * Y, z0 = 2 * Z;
+        const float* b = F.e + lidx(x0, y0, z0, F.nx, F.ny);
+        const float* rb = F.r + lidx(x0, y0, z0, F.nx, F.ny);
+        const long long sy = F.nx, sz = nxy;
+        float E[2][2][2], R[2][2][2];
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    E[dz][dy][dx] = b[dx + dy * sy + dz * sz];
+                    R[dz][dy][dx] = rb[dx + dy * sy + dz * sz];
+                }
+        const bool xl = x0 > 0, xh = x0 + 2 < F.nx, yl = y0 > 0, yh = y0 + 2 < F.ny, zl = z0 > 0, zh = z0 + 2 < F.nz;
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    const long long o = dx + dy * sy + dz * sz;
+                    const float c = E[dz][dy][dx];
+                    const float xm = dx ? E[dz][dy][0] : (xl ? b[o - 1] : c);
+                    const float xp = dx ? (xh ? b[o + 1] : c) : E[dz][dy][1];
+                    const float ym = dy ? E[dz][0][dx] : (yl ? b[o - sy] : c);
+                    const float yp = dy ? (yh ? b[o + sy] : c) : E[dz][1][dx];
+                    const float zm = dz ? E[0][dy][dx] : (zl ? b[o - sz] : c);
+                    const float zp = dz ? (zh ? b[o + sz] : c) : E[1][dy][dx];
+                    sum += mg_res(F, xm + xp, ym + yp, zm + zp, c, R[dz][dy][dx]);
+                }
+    } else {
+        for (int dz = 0; dz < ez; ++dz)
+            for (int dy = 0; dy < ey; ++dy)
+                for (int dx = 0; dx < ex; ++dx) sum += mg_residual(F, X * ex + dx, Y * ey + dy, Z * ez + dz);
+    }
     C.r[el] = sum * inv;
     C.e[el] = 0.0f;
     END_ELEMS
