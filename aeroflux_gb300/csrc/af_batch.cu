@@ -639,12 +639,23 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
     const float* c01 = C.e + lidx(0, Y0, Z1, C.nx, C.ny);
     const float* c11 = C.e + lidx(0, Y1, Z1, C.nx, C.ny);
     float* fe = F.e + lidx(0, y, z, F.nx, F.ny);
-    for (int x = lane; x < F.nx; x += 32) {
-        int X0 = x, X1 = x;
-        float ax = 1.0f;
-        if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
-        fe[x] = __fadd_rn(fe[x], mg_interp(ax, ay, az, c00[X0], c00[X1], c10[X0], c10[X1], c01[X0], c01[X1], c11[X0],
-                                           c11[X1]));
+    if (F.cx) {
+        // A lane owns the fine pair (2X, 2X+1): both take parent X, the even
+        // one neighbour X-1 and the odd one X+1 (clamped at the walls), so
+        // the pair shares its coarse loads and one 8-byte access of e (nx is
+        // even and every row starts on an even element).
+        for (int X = lane; X < C.nx; X += 32) {
+            const int Xm = max(X - 1, 0), Xp = min(X + 1, C.nx - 1);
+            const float a00 = c00[X], a10 = c10[X], a01 = c01[X], a11 = c11[X];
+            float2 f = reinterpret_cast<float2*>(fe)[X];
+            f.x = __fadd_rn(f.x, mg_interp(0.75f, ay, az, a00, c00[Xm], a10, c10[Xm], a01, c01[Xm], a11, c11[Xm]));
+            f.y = __fadd_rn(f.y, mg_interp(0.75f, ay, az, a00, c00[Xp], a10, c10[Xp], a01, c01[Xp], a11, c11[Xp]));
+            reinterpret_cast<float2*>(fe)[X] = f;
+        }
+    } else {
+        for (int x = lane; x < F.nx; x += 32)
+            fe[x] = __fadd_rn(fe[x], mg_interp(1.0f, ay, az, c00[x], c00[x], c10[x], c10[x], c01[x], c01[x], c11[x],
+                                               c11[x]));
     }
     END_ELEMS
     END_TILES
