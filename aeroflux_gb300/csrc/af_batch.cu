@@ -292,7 +292,55 @@ __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
 
 // One axis sweep of every face.  A warp owns one (component, y, z) face row
 // (32 lanes per row of the face box) and its lanes stride over x; taps come
-// from the binary32 shadow.
+// from the binary32 shadow.  Per row the kernel fixes the component (a
+// template parameter), the row pointers of the face's own field and of the
+// axis component that gives the face velocity, and the four 32-bit offsets
+// of that velocity's taps, so a face costs its nine loads, the arithmetic
+// of mx_face_update and one store.
+template <int AX, int C>
+__device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* __restrict__ dd, int y, int z,
+                                          int lane, int phase) {
+    const Geom& g = I.g;
+    const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
+    const Dims& a = AX == 0 ? g.u : (AX == 1 ? g.v : g.w);
+    const long long rb = (long long)y * d.sy + (long long)z * d.sz;
+    const float* __restrict__ src = I.sh[C] + rb;
+    dd += rb;
+    const int s = AX == 0 ? 1 : (AX == 1 ? (int)d.sy : (int)d.sz);
+    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+    // Face velocity taps (mx_face_vel): offsets from (x, y, z) in the axis
+    // component, in the order they are summed.
+    const float* __restrict__ va = I.sh[AX] + (long long)y * a.sy + (long long)z * a.sz;
+    const int ay = (int)a.sy, az = (int)a.sz;
+    int o0 = 0, o1 = 0, o2 = 0, o3 = 0;
+    if (C == 0 && AX == 1) { o0 = -1; o1 = 0; o2 = ay - 1; o3 = ay; }
+    if (C == 0 && AX == 2) { o0 = -1; o1 = 0; o2 = az - 1; o3 = az; }
+    if (C == 1 && AX == 0) { o0 = -ay; o1 = 1 - ay; o2 = 0; o3 = 1; }
+    if (C == 1 && AX == 2) { o0 = -ay; o1 = 0; o2 = az - ay; o3 = az; }
+    if (C == 2 && AX == 0) { o0 = -az; o1 = 1 - az; o2 = 0; o3 = 1; }
+    if (C == 2 && AX == 1) { o0 = -az; o1 = ay - az; o2 = 0; o3 = ay; }
+    const int x0 = g.G + lane, x1 = g.G + g.NX + (C == 0);
+    const float dt_invh = I.dt_invh, lam = I.lam;
+    auto vel_at = [&](int x) {
+        return C == AX ? src[x] : mx_face_vel4(va[x + o0], va[x + o1], va[x + o2], va[x + o3]);
+    };
+    // The next face's velocity taps load before this face's dependent taps,
+    // so a lane keeps two faces' loads in flight.
+    float vel_next = x0 < x1 ? vel_at(x0) : 0.0f;
+    for (int x = x0; x < x1; x += 32) {
+        const float vel = vel_next;
+        if (x + 32 < x1) vel_next = vel_at(x + 32);
+        const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+        float res;
+        if (!mx_face_update(src + x, s, vel, ca, na, dt_invh, lam, &res)) {
+            atomicMin(&st->fault_gate, st->step * 8u + (unsigned)phase);
+            atomicMin(&st->fault_key, fault_key(C, x, y, z));
+            continue;
+        }
+        dd[x] = (double)res;  // widening is exact
+    }
+}
+
 template <int AX>
 __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, int phase) {
     FOR_TILES(tab)
@@ -300,9 +348,6 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
     if (gated(&st[s], phase)) continue;
     const Geom& g = I.g;
     const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1);
-    double* tu = cur(I, 5, parity);
-    double* tv = cur(I, 6, parity);
-    double* tw = cur(I, 7, parity);
     FOR_ELEMS(tab)
     const long long row = el >> 5;
     if (row >= rows) break;
@@ -311,12 +356,9 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
     const int c = (int)cc;
     const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
     if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
-    const int x1 = g.G + g.NX + (c == 0);
-    for (int x = g.G + lane; x < x1; x += 32)
-        if (!mx_sweep_face<AX, float>(g, I.sh[0], I.sh[1], I.sh[2], tu, tv, tw, I.dt_invh, I.lam, c, x, y, z)) {
-            atomicMin(&st[s].fault_gate, st[s].step * 8u + (unsigned)phase);
-            atomicMin(&st[s].fault_key, fault_key(c, x, y, z));
-        }
+    if (c == 0) sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, lane, phase);
+    else if (c == 1) sweep_row<AX, 1>(I, st + s, cur(I, 6, parity), y, z, lane, phase);
+    else sweep_row<AX, 2>(I, st + s, cur(I, 7, parity), y, z, lane, phase);
     END_ELEMS
     END_TILES
 }
@@ -691,10 +733,11 @@ __device__ float block_sum(float v, float* red) {
 // on colour.  Nothing reads what the kernel writes, so blocks never race, and
 // the result equals the two in-place colour sweeps bit for bit (mg_relax in
 // both).  Per pair it moves e and r once and writes e once.
-constexpr int kPairTX = 64, kPairTY = 8, kPairTZ = 8;
+constexpr int kPairTX = 64, kPairTY = 16, kPairTZ = 8;
+constexpr int kPairThreads = 32 * kPairTY;  // a warp per tile row
 constexpr int kPairRX = kPairTX / 2 + 1, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
 
-__global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir,
+__global__ void __launch_bounds__(kPairThreads, 2048 / kPairThreads) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir,
                                                       int vc) {
     __shared__ float red[kPairHZ][kPairHY][kPairRX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -728,8 +771,9 @@ __global__ void __launch_bounds__(256) kb_smooth_pair(const InstDev* inst, const
             }
             red[hz][hy][k] = v;
         };
-        for (int row = warp; row < kPairHY * kPairHZ; row += 8) red_row(row % kPairHY, row / kPairHY, lane);
-        for (int row = tid; row < kPairHY * kPairHZ; row += 256) red_row(row % kPairHY, row / kPairHY, kPairRX - 1);
+        for (int row = warp; row < kPairHY * kPairHZ; row += kPairTY) red_row(row % kPairHY, row / kPairHY, lane);
+        for (int row = tid; row < kPairHY * kPairHZ; row += kPairThreads)
+            red_row(row % kPairHY, row / kPairHY, kPairRX - 1);
         __syncthreads();
         // Output pairs: lane -> x = x0 + 2*lane + {0, 1}, warp -> y, loop over z.
         const int y = y0 + warp, hy = warp + 1;
@@ -1192,7 +1236,8 @@ void enq_smooth(Batch* b, int st, int l, int pairs, int vc, cudaStream_t s) {
 void enq_level_smooth(Batch* b, int l, int vc, cudaStream_t s) {
     if (b->graph_pair & (1u << l))
         for (int k = 0; k < b->nu; ++k) {
-            kb_smooth_pair<<<grid(b, S_PAIR + l), 256, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1, vc);
+            kb_smooth_pair<<<grid(b, S_PAIR + l), kPairThreads, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l,
+                                                                        k & 1, vc);
             ++b->launches;
         }
     if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, vc, s);
@@ -1387,7 +1432,7 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     if (const char* vc = getenv("AEROFLUX_MG_VCYCLES")) b->vcycles = std::min(8, std::max(1, atoi(vc)));
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
-    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{256, 1, 8};
+    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{kPairThreads, 1, 2048 / kPairThreads};
     cudaError_t rc;
     if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||

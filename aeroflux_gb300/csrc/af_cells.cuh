@@ -353,53 +353,33 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 }
 
 // --- binary32 advection + diffusion of one face (stencil.go:44-225) --------
-// Returns false on a NaN backtrace (a contained fault); the face is then not
-// written.  Only the active axis is interpolated: the other two weights are 0.
-// Taps come from the binary64 fields (converted here) or from their binary32
-// shadow (converted once per sweep by the same f64_to_f32): the same values.
-__device__ __forceinline__ float tap32(const double* p, long long i) { return f64_to_f32(p[i]); }
-__device__ __forceinline__ float tap32(const float* p, long long i) { return p[i]; }
+// The sweep interpolates along its axis only (the other two weights are 0).
+// Every rounding is explicit, so the result does not depend on how the
+// compiler contracts multiplies and adds.
 
-template <int AX, class T>
-__device__ __forceinline__ float mx_face_vel(const Geom& g, const T* u, const T* v, const T* w, int c, int x, int y,
-                                             int z) {
-    auto U = [&](int i, int j, int k) { return tap32(u, i + j * g.u.sy + k * g.u.sz); };
-    auto V = [&](int i, int j, int k) { return tap32(v, i + j * g.v.sy + k * g.v.sz); };
-    auto W = [&](int i, int j, int k) { return tap32(w, i + j * g.w.sy + k * g.w.sz); };
-    if (c == 0) {
-        if (AX == 0) return U(x, y, z);
-        if (AX == 1) return 0.25f * (V(x - 1, y, z) + V(x, y, z) + V(x - 1, y + 1, z) + V(x, y + 1, z));
-        return 0.25f * (W(x - 1, y, z) + W(x, y, z) + W(x - 1, y, z + 1) + W(x, y, z + 1));
-    } else if (c == 1) {
-        if (AX == 0) return 0.25f * (U(x, y - 1, z) + U(x + 1, y - 1, z) + U(x, y, z) + U(x + 1, y, z));
-        if (AX == 1) return V(x, y, z);
-        return 0.25f * (W(x, y - 1, z) + W(x, y, z) + W(x, y - 1, z + 1) + W(x, y, z + 1));
-    } else {
-        if (AX == 0) return 0.25f * (U(x, y, z - 1) + U(x + 1, y, z - 1) + U(x, y, z) + U(x + 1, y, z));
-        if (AX == 1) return 0.25f * (V(x, y, z - 1) + V(x, y + 1, z - 1) + V(x, y, z) + V(x, y + 1, z));
-        return W(x, y, z);
-    }
+// Face velocity from the four axis-component faces around it, summed in the
+// order given: 0.25 * (((t0 + t1) + t2) + t3).
+__device__ __forceinline__ float mx_face_vel4(float t0, float t1, float t2, float t3) {
+    return __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3));
 }
 
-template <int AX, class T>
-__device__ __forceinline__ bool mx_sweep_face(const Geom& g, const T* u, const T* v, const T* w, double* tu,
-                                              double* tv, double* tw, float dt_invh, float lam, int c, int x, int y,
-                                              int z) {
-    const Dims& d = c == 0 ? g.u : (c == 1 ? g.v : g.w);
-    const T* sd = c == 0 ? u : (c == 1 ? v : w);
-    double* dd = c == 0 ? tu : (c == 1 ? tv : tw);
-    const float vel = mx_face_vel<AX, T>(g, u, v, w, c, x, y, z);
-    // Backtrace relative to the face, so binary32 keeps the fraction accurate
-    // at any grid size: departure = face + off, off = -dt*v/h.
-    const int ca = AX == 0 ? x : (AX == 1 ? y : z);
-    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
-    const float off = -(vel * dt_invh);
+// New value of the face whose binary32 value sits at f[0] (its neighbours
+// along the sweep axis at f[-s] and f[s]; ca is its coordinate on that axis,
+// na the field's padded extent there): the semi-Lagrangian backtrace by
+// velocity vel, relative to the face so binary32 keeps the fraction accurate
+// at any grid size (departure = ca + off, off = -dt*vel/h), clamped into the
+// padded field as stencil.go:174-188 clamps, linear interpolation
+// d0 + t*(d1 - d0), plus lam times the second difference.  Returns false on
+// a NaN backtrace (a contained fault; the face is then not written).
+__device__ __forceinline__ bool mx_face_update(const float* __restrict__ f, int s, float vel, int ca, int na,
+                                               float dt_invh, float lam, float* out) {
+    const float off = -__fmul_rn(vel, dt_invh);
     if (isnan(off)) return false;
     const float fl = floorf(off);
-    const float pos = (float)ca + off;
+    const float pos = __fadd_rn((float)ca, off);
     int i0;
     float t;
-    if (!(pos > 0.0f)) {  // clamp into the padded field (stencil.go:174-188)
+    if (!(pos > 0.0f)) {
         i0 = 0;
         t = 0.0f;
     } else if (pos >= (float)(na - 1)) {
@@ -407,22 +387,17 @@ __device__ __forceinline__ bool mx_sweep_face(const Geom& g, const T* u, const T
         t = 1.0f;
     } else {
         i0 = ca + (int)fl;
-        t = off - fl;
-        if (i0 >= na - 1) { i0 = na - 2; t = 1.0f; }
+        t = __fsub_rn(off, fl);
+        if (i0 >= na - 1) {
+            i0 = na - 2;
+            t = 1.0f;
+        }
     }
-    const long long s = AX == 0 ? 1 : (AX == 1 ? d.sy : d.sz);
-    const long long base = (long long)x + (long long)y * d.sy + (long long)z * d.sz;
-    const long long j0 = base + (long long)(i0 - ca) * s;
-    const float d0 = tap32(sd, j0), d1 = tap32(sd, j0 + s);
-    const float adv = fmaf(t, d1 - d0, d0);
-    float lap = 0.0f;
-    if (lam != 0.0f) {
-        const float c0 = tap32(sd, base);
-        lap = lam * ((tap32(sd, base - s) - 2.0f * c0) + tap32(sd, base + s));
-    }
-    // Widening is exact; the sweep leaves the FP64 pipe idle, so the native
-    // conversion (one instruction) beats the integer form here.
-    dd[base] = (double)(adv + lap);
+    const float* p0 = f + (long long)(i0 - ca) * s;
+    const float d0 = p0[0], d1 = p0[s];
+    const float adv = __fmaf_rn(t, __fsub_rn(d1, d0), d0);
+    if (lam != 0.0f) *out = __fmaf_rn(lam, __fadd_rn(__fsub_rn(f[-s], __fmul_rn(2.0f, f[0])), f[s]), adv);
+    else *out = __fadd_rn(adv, 0.0f);
     return true;
 }
 
