@@ -67,7 +67,8 @@ struct Lvl {
     float* r;
     FastDiv fnx, fny, fhx;  // nx, ny, (nx+1)/2
     float* e2;              // second buffer of the fused red-black pair (levels below the tail)
-    FastDiv ftx, fty;       // fused-pair tiles along x and y
+    FastDiv ftx, fty;       // fused-pair wide tiles along x and tiles along y
+    int nxw;                // 64 x the wide pair tiles along x; a narrow tile column covers nxw .. nx-1
 };
 
 struct Ctl {
@@ -117,7 +118,8 @@ enum {
     S_PROLONG = S_RESTRICT + kMaxLev,
     S_BIGCOARSE = S_PROLONG + kMaxLev,
     S_PAIR = S_BIGCOARSE + kMaxLev,
-    S_COUNT = S_PAIR + kMaxLev
+    S_PAIRN = S_PAIR + kMaxLev,
+    S_COUNT = S_PAIRN + kMaxLev
 };
 
 struct Shape {
@@ -724,8 +726,8 @@ __device__ float block_sum(float v, float* red) {
 // One red sweep then one black sweep of L e = r, from e_in into e_out.  The
 // red values read only e_in (their black neighbours are unchanged by the red
 // sweep); the black values read the new red values.  Each block owns an
-// output tile of kPairTX x kPairTY x kPairTZ cells.  It first computes the
-// new red values of the tile plus a one-cell halo -- only the red cells, kept
+// output tile of TX x kPairTY x kPairTZ cells.  It first computes the new
+// red values of the tile plus a one-cell halo -- only the red cells, kept
 // compactly in shared memory (a row of the halo alternates colours, so
 // x >> 1 indexes its red cells) -- then, after one barrier, each lane writes
 // an adjacent (x, x+1) pair of the tile, one red cell (from shared memory)
@@ -733,14 +735,31 @@ __device__ float block_sum(float v, float* red) {
 // on colour.  Nothing reads what the kernel writes, so blocks never race, and
 // the result equals the two in-place colour sweeps bit for bit (mg_relax in
 // both).  Per pair it moves e and r once and writes e once.
-constexpr int kPairTX = 64, kPairTY = 16, kPairTZ = 8;
-constexpr int kPairThreads = 32 * kPairTY;  // a warp per tile row
-constexpr int kPairRX = kPairTX / 2 + 1, kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
+//
+// Wide tiles (LANES = 32, TX = 64, a warp per row) cover x < nxw; a level
+// whose x extent leaves 1..32 cells past the last wide tile (nx = 32, 96,
+// ...) covers them with one narrow tile column (LANES = 16, TX = 32, a warp
+// per two rows) instead of a half-idle wide tile.
+constexpr int kPairTY = 16, kPairTZ = 8;
+constexpr int kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
+constexpr int kPairWideX = 64;
 
-__global__ void __launch_bounds__(kPairThreads, 2048 / kPairThreads) kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir,
-                                                      int vc) {
-    __shared__ float red[kPairHZ][kPairHY][kPairRX];
+template <int LANES>
+struct PairTile {
+    static constexpr int TX = 2 * LANES;        // cells along x
+    static constexpr int RX = LANES + 1;        // red cells of a halo row
+    static constexpr int RPW = 32 / LANES;      // tile rows per warp
+    static constexpr int THREADS = kPairTY * LANES;
+};
+
+template <int LANES>
+__global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANES>::THREADS)
+    kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir, int vc) {
+    using T = PairTile<LANES>;
+    __shared__ float red[kPairHZ][kPairHY][T::RX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int k = lane % LANES;                        // pair of the row
+    const int wrow = warp * T::RPW + lane / LANES;     // tile row, 0 .. kPairTY-1
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (mg_off(ctl[s], vc)) continue;
@@ -750,16 +769,26 @@ __global__ void __launch_bounds__(kPairThreads, 2048 / kPairThreads) kb_smooth_p
         const float* __restrict__ r = L.r;
         const int nx = L.nx, ny = L.ny, nz = L.nz, nxy = nx * ny;  // a level holds < 2^31 cells
         const unsigned local = (unsigned)(item - tab.prefix[s]);
-        const unsigned q1 = L.ftx.div(local), q2 = L.fty.div(q1);
-        const int bx = (int)(local - q1 * L.ftx.d), by = (int)(q1 - q2 * L.fty.d), bz = (int)q2;
-        const int x0 = bx * kPairTX, y0 = by * kPairTY, z0 = bz * kPairTZ;
+        int x0, y0, z0;
+        if (LANES == 32) {
+            const unsigned q1 = L.ftx.div(local), q2 = L.fty.div(q1);
+            x0 = (int)(local - q1 * L.ftx.d) * T::TX;
+            y0 = (int)(q1 - q2 * L.fty.d) * kPairTY;
+            z0 = (int)q2 * kPairTZ;
+        } else {
+            const unsigned q2 = L.fty.div(local);
+            x0 = L.nxw;
+            y0 = (int)(local - q2 * L.fty.d) * kPairTY;
+            z0 = (int)q2 * kPairTZ;
+        }
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        // Red cells of the halo tile, one warp per halo row (hy, hz): halo
-        // x = x0 - 1 + hx, hx = 2k + ((y + z + 1) & 1); lanes take k < 32 and
-        // the rows' last cells (k = 32) go one per thread afterwards.
-        auto red_row = [&](int hy, int hz, int k) {
+        // Red cells of the halo tile, a row of lanes per halo row (hy, hz):
+        // halo x = x0 - 1 + hx, hx = 2j + ((y + z + 1) & 1); lanes take
+        // j < LANES and the rows' last cells (j = LANES) go one per thread
+        // afterwards.
+        auto red_row = [&](int hy, int hz, int j) {
             const int y = y0 - 1 + hy, z = z0 - 1 + hz;
-            const int x = x0 - 1 + 2 * k + ((y + z + 1) & 1);
+            const int x = x0 - 1 + 2 * j + ((y + z + 1) & 1);
             float v = 0.0f;
             if ((unsigned)x < (unsigned)nx && (unsigned)y < (unsigned)ny && (unsigned)z < (unsigned)nz) {
                 const int i = x + nx * y + nxy * z;
@@ -769,15 +798,15 @@ __global__ void __launch_bounds__(kPairThreads, 2048 / kPairThreads) kb_smooth_p
                 const float* p = ein + i;
                 v = mg_relax(L, p[oxm] + p[oxp], p[oym] + p[oyp], p[ozm] + p[ozp], r[i], inv, p[0]);
             }
-            red[hz][hy][k] = v;
+            red[hz][hy][j] = v;
         };
-        for (int row = warp; row < kPairHY * kPairHZ; row += kPairTY) red_row(row % kPairHY, row / kPairHY, lane);
-        for (int row = tid; row < kPairHY * kPairHZ; row += kPairThreads)
-            red_row(row % kPairHY, row / kPairHY, kPairRX - 1);
+        for (int row = wrow; row < kPairHY * kPairHZ; row += kPairTY) red_row(row % kPairHY, row / kPairHY, k);
+        for (int row = tid; row < kPairHY * kPairHZ; row += T::THREADS)
+            red_row(row % kPairHY, row / kPairHY, LANES);
         __syncthreads();
-        // Output pairs: lane -> x = x0 + 2*lane + {0, 1}, warp -> y, loop over z.
-        const int y = y0 + warp, hy = warp + 1;
-        const int xa = x0 + 2 * lane;
+        // Output pairs: lane k -> x = x0 + 2k + {0, 1}, tile row -> y, loop over z.
+        const int y = y0 + wrow, hy = wrow + 1;
+        const int xa = x0 + 2 * k;
         if (y < ny && xa < nx) {
             const int zend = min(kPairTZ, nz - z0);
             int i0 = xa + nx * y + nxy * z0;
@@ -1068,7 +1097,8 @@ struct Batch {
     int grid_sz[S_COUNT] = {};       // blocks per stage, fixed when the graph is captured
     int graph_levels = 0;            // levels the captured graph covers
     unsigned graph_big = 0;          // levels whose large-coarsest smoothing the graph carries
-    unsigned graph_pair = 0;         // levels with fused-pair smoothing in the graph
+    unsigned graph_pair = 0;         // levels with wide fused-pair tiles in the graph
+    unsigned graph_pairn = 0;        // levels with narrow fused-pair tiles in the graph
     unsigned graph_single = 0;       // levels with in-place colour sweeps in the graph
     size_t tail_smem = 0;            // dynamic shared memory of the tail V-cycle
     int graph_nu = 0;                // smoothing sweeps the captured graph carries
@@ -1116,6 +1146,20 @@ unsigned smooth_levels(const Batch* b, bool pair) {
     return m;
 }
 
+// Levels whose fused pairs need the narrow tile column (wide: the others).
+unsigned pair_levels(const Batch* b, bool narrow) {
+    unsigned m = 0;
+    for (const auto& s : b->slots) {
+        if (!s.used) continue;
+        const int lim = s.d.tail >= 0 ? s.d.tail : s.d.nlev - 1;
+        for (int l = 0; l < lim; ++l) {
+            const Lvl& L = s.d.lev[l];
+            if (L.e2 && (narrow ? L.nxw < L.nx : L.nxw > 0)) m |= 1u << l;
+        }
+    }
+    return m;
+}
+
 size_t tail_smem_bytes(const Batch* b) {
     size_t m = 0;
     for (const auto& s : b->slots)
@@ -1153,10 +1197,12 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
         const int l = st - S_BIGCOARSE;
         n = (l == I.nlev - 1 && I.tail < 0) ? row_box(I.lev[l]) : 0;
     } else if (st >= S_PAIR && st < S_COUNT) {
-        const int l = st - S_PAIR;
+        const bool wide = st < S_PAIRN;
+        const int l = st - (wide ? S_PAIR : S_PAIRN);
         if (l >= lim || !I.lev[l].e2) return 0;
         const Lvl& L = I.lev[l];
-        return cdivl(L.nx, kPairTX) * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairTZ);
+        const long long cols = wide ? L.nxw / kPairWideX : (L.nxw < L.nx ? 1 : 0);
+        return cols * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairTZ);
     }
     return cdivl(n, per);
 }
@@ -1234,12 +1280,20 @@ void enq_smooth(Batch* b, int st, int l, int pairs, int vc, cudaStream_t s) {
 // (an even count returns the result to e) for slots that have e2, in-place
 // colour sweeps for the others.
 void enq_level_smooth(Batch* b, int l, int vc, cudaStream_t s) {
-    if (b->graph_pair & (1u << l))
-        for (int k = 0; k < b->nu; ++k) {
-            kb_smooth_pair<<<grid(b, S_PAIR + l), kPairThreads, 0, s>>>(b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l,
-                                                                        k & 1, vc);
+    // A pair reads the previous pair's output across the wide / narrow
+    // boundary, so both kinds finish pair k before either starts pair k+1.
+    for (int k = 0; k < b->nu; ++k) {
+        if (b->graph_pair & (1u << l)) {
+            kb_smooth_pair<32><<<grid(b, S_PAIR + l), PairTile<32>::THREADS, 0, s>>>(
+                b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1, vc);
             ++b->launches;
         }
+        if (b->graph_pairn & (1u << l)) {
+            kb_smooth_pair<16><<<grid(b, S_PAIRN + l), PairTile<16>::THREADS, 0, s>>>(
+                b->d_inst, b->d_ctl, tab(b, S_PAIRN + l), l, k & 1, vc);
+            ++b->launches;
+        }
+    }
     if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, vc, s);
 }
 
@@ -1376,10 +1430,12 @@ cudaError_t prepare(Batch* b) {
     cudaError_t rc;
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     const int L = max_levels(b);
-    const unsigned big = big_coarse_levels(b), pair = smooth_levels(b, true), single = smooth_levels(b, false);
+    const unsigned big = big_coarse_levels(b), pair = pair_levels(b, false), pairn = pair_levels(b, true),
+                   single = smooth_levels(b, false);
     const size_t tsm = tail_smem_bytes(b);
     if (b->graph && (L > b->graph_levels || (big & ~b->graph_big) || (pair & ~b->graph_pair) ||
-                     (single & ~b->graph_single) || tsm > b->tail_smem || b->graph_nu != b->nu)) {
+                     (pairn & ~b->graph_pairn) || (single & ~b->graph_single) || tsm > b->tail_smem ||
+                     b->graph_nu != b->nu)) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
@@ -1387,6 +1443,7 @@ cudaError_t prepare(Batch* b) {
         b->graph_levels = std::max(L, b->graph_levels);
         b->graph_big |= big;
         b->graph_pair |= pair;
+        b->graph_pairn |= pairn;
         b->graph_single |= single;
         b->tail_smem = std::max(b->tail_smem, tsm);
         b->graph_nu = b->nu;
@@ -1432,7 +1489,10 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     if (const char* vc = getenv("AEROFLUX_MG_VCYCLES")) b->vcycles = std::min(8, std::max(1, atoi(vc)));
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
-    for (int l = 0; l < kMaxLev; ++l) b->shape[S_PAIR + l] = Shape{kPairThreads, 1, 2048 / kPairThreads};
+    for (int l = 0; l < kMaxLev; ++l) {
+        b->shape[S_PAIR + l] = Shape{PairTile<32>::THREADS, 1, 2048 / PairTile<32>::THREADS};
+        b->shape[S_PAIRN + l] = Shape{PairTile<16>::THREADS, 1, 2048 / PairTile<16>::THREADS};
+    }
     cudaError_t rc;
     if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -1481,6 +1541,13 @@ void batch_destroy(Batch* b) {
 
 namespace {
 
+// x extent covered by wide pair tiles: every whole 64 plus a last partial
+// one of more than 32 cells; 1..32 remaining cells go to a narrow tile.
+int pair_wide_x(int nx) {
+    const int w = nx / kPairWideX * kPairWideX;
+    return nx - w > kPairWideX / 2 ? w + kPairWideX : w;
+}
+
 // Multigrid hierarchy of a grid: coarsen every axis whose extent is even and
 // >= 4 until the grid has <= 64 cells or no axis halves.
 int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
@@ -1490,7 +1557,8 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
         Lvl& L = lev[n++];
         L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr,
                 FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr,
-                FastDiv((unsigned)((nx + kPairTX - 1) / kPairTX)), FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY))};
+                FastDiv((unsigned)std::max(1, pair_wide_x(nx) / kPairWideX)),
+                FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY)), pair_wide_x(nx)};
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
         if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;
@@ -1740,7 +1808,8 @@ cudaError_t batch_prepare_capture(Batch* b) {
     }
     b->graph_levels = std::max(b->graph_levels, max_levels(b));
     b->graph_big |= big_coarse_levels(b);
-    b->graph_pair |= smooth_levels(b, true);
+    b->graph_pair |= pair_levels(b, false);
+    b->graph_pairn |= pair_levels(b, true);
     b->graph_single |= smooth_levels(b, false);
     b->tail_smem = std::max(b->tail_smem, tail_smem_bytes(b));
     if ((rc = cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem)) !=

@@ -94,10 +94,13 @@ def run_steps(n, steps, per_level, pairs):
     return out
 
 
-@pytest.mark.parametrize("n", [(32, 32, 32), (48, 32, 96), (64, 64, 64), (33, 17, 20), (160, 176, 144)])
+@pytest.mark.parametrize("n", [(32, 32, 32), (48, 32, 96), (64, 64, 64), (33, 17, 20), (160, 176, 144),
+                               (96, 40, 36), (16, 24, 40)])
 def test_fused_pairs_and_tail_vcycle_equal_per_level_kernels(n):
-    # The fused red-black pair and the one-block tail V-cycle reorganise the
-    # per-level colour sweeps without changing any rounding: identical bits.
+    # The fused red-black pair (wide 64-cell and narrow 32-cell tile columns,
+    # both within one level where nx = 64k + 1..32) and the one-block tail
+    # V-cycle reorganise the per-level colour sweeps without changing any
+    # rounding: identical bits.
     ref = run_steps(n, 2, True, False)
     assert np.array_equal(run_steps(n, 2, False, False), ref)
     assert np.array_equal(run_steps(n, 2, False, True), ref)
