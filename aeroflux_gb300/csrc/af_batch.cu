@@ -660,18 +660,31 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l,
 
 // e_fine += cell-centred trilinear interpolation of e_coarse: per coarsened
 // axis the parent weighs 3/4 and the next coarse cell toward the fine cell
-// 1/4 (clamped at the walls, the Neumann reflection).  A warp owns one fine
-// (y, z) row (row_box of the fine level); its four coarse rows are fixed.
+// 1/4 (clamped at the walls, the Neumann reflection).  A row of 2^lg lanes
+// owns one fine (y, z) row, whose four coarse rows are fixed; short rows
+// (at most 16 lane iterations) share a warp two or four to a warp, so the
+// per-row setup is not paid by idle lanes.  The iteration space counts 32
+// lanes per warp (prolong_box).
+__host__ __device__ inline int prolong_lanes_log(const Lvl& F, const Lvl& C) {
+    const int w = F.cx ? C.nx : F.nx;  // lane iterations of a row
+    return w > 16 ? 5 : (w > 8 ? 4 : 3);
+}
+__host__ __device__ inline long long prolong_box(const Lvl& F, const Lvl& C) {
+    const int sh = 5 - prolong_lanes_log(F, C);
+    return 32ll * ((((long long)F.ny * F.nz) + (1 << sh) - 1) >> sh);
+}
+
 __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
     FOR_TILES(tab)
     if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
     const Lvl C = inst[s].lev[l + 1];
     const long long rows = (long long)F.ny * F.nz;
+    const int lg = prolong_lanes_log(F, C), lanes = 1 << lg;
     FOR_ELEMS(tab)
-    const long long row = el >> 5;
+    const long long row = ((el >> 5) << (5 - lg)) + ((el & 31) >> lg);
     if (row >= rows) break;
-    const int lane = (int)(el & 31);
+    const int lane = (int)(el & (lanes - 1));
     const unsigned zz = F.fny.div((unsigned)row);
     const int y = (int)((unsigned)row - zz * (unsigned)F.ny), z = (int)zz;
     int Y0 = y, Y1 = y, Z0 = z, Z1 = z;
@@ -688,7 +701,7 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
         // one neighbour X-1 and the odd one X+1 (clamped at the walls), so
         // the pair shares its coarse loads and one 8-byte access of e (nx is
         // even and every row starts on an even element).
-        for (int X = lane; X < C.nx; X += 32) {
+        for (int X = lane; X < C.nx; X += lanes) {
             const int Xm = max(X - 1, 0), Xp = min(X + 1, C.nx - 1);
             const float a00 = c00[X], a10 = c10[X], a01 = c01[X], a11 = c11[X];
             float2 f = reinterpret_cast<float2*>(fe)[X];
@@ -697,7 +710,7 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
             reinterpret_cast<float2*>(fe)[X] = f;
         }
     } else {
-        for (int x = lane; x < F.nx; x += 32)
+        for (int x = lane; x < F.nx; x += lanes)
             fe[x] = __fadd_rn(fe[x], mg_interp(1.0f, ay, az, c00[x], c00[x], c10[x], c10[x], c01[x], c01[x], c11[x],
                                                c11[x]));
     }
@@ -1192,7 +1205,7 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
         n = l < lim ? lvl_cells(I.lev[l + 1]) : 0;
     } else if (st >= S_PROLONG && st < S_BIGCOARSE) {
         const int l = st - S_PROLONG;
-        n = l < lim ? row_box(I.lev[l]) : 0;
+        n = l < lim ? prolong_box(I.lev[l], I.lev[l + 1]) : 0;
     } else if (st >= S_BIGCOARSE && st < S_PAIR) {
         const int l = st - S_BIGCOARSE;
         n = (l == I.nlev - 1 && I.tail < 0) ? row_box(I.lev[l]) : 0;

@@ -207,29 +207,38 @@ __device__ __forceinline__ double bc_src(const BcComp& c, int G, int n, int a, i
 
 // Writes element i (< bc_set_count) of write set `set` of one component:
 // 0 = wall faces, 1 = ghosts of the first tangential axis, 2 = ghosts of the
-// second tangential axis (edges included).
-__device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long long i) {
+// second tangential axis (edges included).  A set holds fewer than 2^32
+// elements (2 (N+2)^2 for extents N below 46000), so the index decoding
+// divides in 32 bits.
+__device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long long il) {
+    const unsigned i = (unsigned)il;
     int n, t1, t2;
     double val;
     if (set == 0) {
-        t1 = G + (int)(i % c.N1);
-        const long long r = i / c.N1;
-        t2 = G + (int)(r % c.N2);
-        n = (r / c.N2) ? G + c.Nn : G;
+        const unsigned n1 = (unsigned)c.N1, n2 = (unsigned)c.N2;
+        const unsigned r = i / n1;
+        t1 = G + (int)(i - r * n1);
+        const unsigned q = r / n2;
+        t2 = G + (int)(r - q * n2);
+        n = q ? G + c.Nn : G;
         val = 0.0;
     } else if (set == 1) {
-        n = G + (int)(i % (c.Nn + 1));
-        const long long r = i / (c.Nn + 1);
-        t2 = G + (int)(r % c.N2);
-        const int side = (int)(r / c.N2);
+        const unsigned nn = (unsigned)(c.Nn + 1), n2 = (unsigned)c.N2;
+        const unsigned r = i / nn;
+        n = G + (int)(i - r * nn);
+        const unsigned q = r / n2;
+        t2 = G + (int)(r - q * n2);
+        const int side = (int)q;
         t1 = side ? G + c.N1 : G - 1;
         const int s1 = side ? G + c.N1 - 1 : G;
         val = flip(bc_src(c, G, n, s1, t2));
     } else {
-        n = G + (int)(i % (c.Nn + 1));
-        const long long r = i / (c.Nn + 1);
-        t1 = G - 1 + (int)(r % (c.N1 + 2));
-        const int side = (int)(r / (c.N1 + 2));
+        const unsigned nn = (unsigned)(c.Nn + 1), n1 = (unsigned)(c.N1 + 2);
+        const unsigned r = i / nn;
+        n = G + (int)(i - r * nn);
+        const unsigned q = r / n1;
+        t1 = G - 1 + (int)(r - q * n1);
+        const int side = (int)q;
         t2 = side ? G + c.N2 : G - 1;
         const int s2 = side ? G + c.N2 - 1 : G;
         int s1 = t1;
@@ -255,24 +264,26 @@ __device__ __forceinline__ long long pbc_set_count(const Geom& g, int set) {
     return set == 0 ? 2ll * g.NY * g.NZ : (set == 1 ? 2ll * (g.NX + 2) * g.NZ : 2ll * (g.NX + 2) * (g.NY + 2));
 }
 
-__device__ __forceinline__ void pbc_cell(const Geom& g, double* p, int set, long long i) {
+// A set holds fewer than 2^32 elements: 32-bit index decoding.
+__device__ __forceinline__ void pbc_cell(const Geom& g, double* p, int set, long long il) {
     const int G = g.G, NX = g.NX, NY = g.NY, NZ = g.NZ;
+    const unsigned i = (unsigned)il;
     int x, y, z;
     if (set == 0) {
-        y = G + (int)(i % NY);
-        const long long r = i / NY;
-        z = G + (int)(r % NZ);
-        x = (r / NZ) ? G + NX : G - 1;
+        const unsigned r = i / (unsigned)NY, q = r / (unsigned)NZ;
+        y = G + (int)(i - r * (unsigned)NY);
+        z = G + (int)(r - q * (unsigned)NZ);
+        x = q ? G + NX : G - 1;
     } else if (set == 1) {
-        x = G - 1 + (int)(i % (NX + 2));
-        const long long r = i / (NX + 2);
-        z = G + (int)(r % NZ);
-        y = (r / NZ) ? G + NY : G - 1;
+        const unsigned r = i / (unsigned)(NX + 2), q = r / (unsigned)NZ;
+        x = G - 1 + (int)(i - r * (unsigned)(NX + 2));
+        z = G + (int)(r - q * (unsigned)NZ);
+        y = q ? G + NY : G - 1;
     } else {
-        x = G - 1 + (int)(i % (NX + 2));
-        const long long r = i / (NX + 2);
-        y = G - 1 + (int)(r % (NY + 2));
-        z = (r / (NY + 2)) ? G + NZ : G - 1;
+        const unsigned r = i / (unsigned)(NX + 2), q = r / (unsigned)(NY + 2);
+        x = G - 1 + (int)(i - r * (unsigned)(NX + 2));
+        y = G - 1 + (int)(r - q * (unsigned)(NY + 2));
+        z = q ? G + NZ : G - 1;
     }
     const int cx = min(max(x, G), G + NX - 1);
     const int cy = min(max(y, G), G + NY - 1);
