@@ -469,7 +469,7 @@ __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
 // One block: per slot, whether another refinement pass runs; the WHILE
 // condition is "any slot continues".  Bounded by each slot's max_refine.
 __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaGraphConditionalHandle h, int use_cond,
-                         int count_pass, int gate, int vcycles) {
+                         int count_pass, int gate, int vcycles, double pass_floor) {
     int any = 0;
     for (int s = threadIdx.x; s < n; s += blockDim.x) {
         const InstDev& I = inst[s];
@@ -499,10 +499,16 @@ __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaG
             const double f = pow(div / prev, 1.0 / ran);
             if (f < 1.0) c.vfac = f;
         }
+        // A pass cannot take max|r| below its binary32 floor (the inner
+        // solve's correction carries about 24 bits), so V-cycles past
+        // log(pass_floor) / log(vfac) are cut as well (pass_floor = 0: no
+        // such cut).
         unsigned nv = 0u;
         if (more && c.vfac > 0.0 && c.vfac < 1.0) {
-            const double k = ceil(log(0.5 * I.thresh / div) / log(c.vfac));
-            if (k >= 1.0 && k < (double)vcycles) nv = (unsigned)k;
+            double k = ceil(log(0.5 * I.thresh / div) / log(c.vfac));
+            if (pass_floor > 0.0) k = fmin(k, ceil(log(pass_floor) / log(c.vfac)));
+            if (k < 1.0) k = 1.0;
+            if (k < (double)vcycles) nv = (unsigned)k;
         }
         c.nv = nv;
         if (!more) c.stopped = 1;
@@ -1125,6 +1131,7 @@ struct Batch {
     int64_t launches = 0;
     int nu = 2;
     int vcycles = 4;  // V-cycles per refinement pass at most (measured best of 2, 3, 4, 6, 8)
+    double pass_floor = 0.0;  // max|r| reduction one pass can reach (0: not used to cut V-cycles)
     int fixed_passes = 0;
     cudaError_t capture_err = cudaSuccess;
 };
@@ -1333,7 +1340,7 @@ void enq_pass(Batch* b, cudaStream_t s, cudaGraphConditionalHandle h, int use_co
     for (int k = 0; k < b->vcycles; ++k) enq_vcycle(b, k, s);
     LAUNCH(b, S_CORR, kb_correct, b->d_inst, b->d_ctl, tab(b, S_CORR));
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 1);
-    kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate, b->vcycles);
+    kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, use_cond, 1, gate, b->vcycles, b->pass_floor);
     ++b->launches;
 }
 
@@ -1346,7 +1353,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
     ++b->launches;
     LAUNCH(b, S_INT, kb_residual, b->d_inst, b->d_st, b->d_ctl, tab(b, S_INT), gate, 0);
     if (b->fixed_passes > 0) {
-        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, 0, 0, 0, gate, b->vcycles);
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, 0, 0, 0, gate, b->vcycles, b->pass_floor);
         ++b->launches;
         for (int k = 0; k < b->fixed_passes; ++k) enq_pass(b, s, 0, 0, gate);
     } else {
@@ -1364,7 +1371,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
             b->capture_err = rc;
             return;
         }
-        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, 1, 0, gate, b->vcycles);
+        kb_check<<<1, 256, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, b->cap, h, 1, 0, gate, b->vcycles, b->pass_floor);
         ++b->launches;
         if ((rc = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps)) != cudaSuccess) {
             b->capture_err = rc;
@@ -1500,6 +1507,7 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     // the fixed sweep count of the red-black solver).
     if (const char* cs = getenv("AEROFLUX_COLD_START")) b->cold = atoi(cs) != 0;
     if (const char* vc = getenv("AEROFLUX_MG_VCYCLES")) b->vcycles = std::min(8, std::max(1, atoi(vc)));
+    if (const char* pf = getenv("AEROFLUX_MG_PASS_FLOOR")) b->pass_floor = atoi(pf) < 0 ? ldexp(1.0, atoi(pf)) : 0.0;
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) {
@@ -1562,7 +1570,11 @@ int pair_wide_x(int nx) {
 }
 
 // Multigrid hierarchy of a grid: coarsen every axis whose extent is even and
-// >= 4 until the grid has <= 64 cells or no axis halves.
+// >= 4 until the grid has <= kCoarsestCells cells or no axis halves.  Going
+// down to 8 cells instead of 64 measured 0.2-2 % faster (256^3, 512^3, the
+// 256-grid batch): the coarsest red-black solve (2 nmax^2 pairs, at least 8)
+// is shorter on the smaller grid.
+constexpr long long kCoarsestCells = 8;
 int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
     int n = 0;
     float wx = 1.0f, wy = 1.0f, wz = 1.0f;
@@ -1574,7 +1586,7 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
                 FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY)), pair_wide_x(nx)};
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
-        if (c <= 64 || !(cx || cy || cz) || n == kMaxLev) break;
+        if (c <= kCoarsestCells || !(cx || cy || cz) || n == kMaxLev) break;
         L.cx = cx;
         L.cy = cy;
         L.cz = cz;
