@@ -83,6 +83,10 @@ struct Ctl {
 
 // Whether the multigrid kernels of V-cycle vc of a pass skip a slot.
 __device__ __forceinline__ bool mg_off(const Ctl& c, int vc) { return c.stopped || (c.nv && (unsigned)vc >= c.nv); }
+// ctl[n] (n = the batch's capacity) is the batch's own record: its nv is the
+// number of V-cycles some slot runs in the current pass, so a V-cycle no
+// slot runs returns at once instead of walking the slots' tiles.
+__device__ __forceinline__ bool vc_idle(const Ctl* ctl, int n, int vc) { return (unsigned)vc >= ctl[n].nv; }
 
 struct InstDev {
     Geom g;
@@ -372,6 +376,7 @@ __global__ void kb_tick(const InstDev* inst, Status* st, int n) {
 
 // --- refinement control ---------------------------------------------------
 __global__ void kb_init(const InstDev* inst, Ctl* ctl, int n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl[n].nv = 0xFFFFFFFFu;  // until a check counts them
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         ctl[s].maxr_bits = 0;
         ctl[s].passes = 0;
@@ -470,6 +475,9 @@ __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
 // condition is "any slot continues".  Bounded by each slot's max_refine.
 __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaGraphConditionalHandle h, int use_cond,
                          int count_pass, int gate, int vcycles, double pass_floor) {
+    __shared__ unsigned most;  // V-cycles of the next pass, most over the slots
+    if (threadIdx.x == 0) most = 0u;
+    __syncthreads();
     int any = 0;
     for (int s = threadIdx.x; s < n; s += blockDim.x) {
         const InstDev& I = inst[s];
@@ -512,9 +520,11 @@ __global__ void kb_check(const InstDev* inst, Status* st, Ctl* ctl, int n, cudaG
         }
         c.nv = nv;
         if (!more) c.stopped = 1;
+        else atomicMax(&most, nv ? nv : (unsigned)vcycles);
         any |= more ? 1 : 0;
     }
     any = __syncthreads_or(any);
+    if (threadIdx.x == 0) ctl[n].nv = most;
     if (threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
@@ -560,6 +570,7 @@ __device__ __forceinline__ float mg_interp(float ax, float ay, float az, float e
 __host__ __device__ inline long long row_box(const Lvl& L) { return 32ll * L.ny * L.nz; }
 
 __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int color, int vc) {
+    if (vc_idle(ctl, tab.n, vc)) return;
     FOR_TILES(tab)
     if (mg_off(ctl[s], vc)) continue;
     const Lvl L = inst[s].lev[l];
@@ -604,6 +615,7 @@ __device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) 
 // Coarse rhs = mean of the children's residuals; coarse solution = 0.  One
 // thread per coarse cell (row-wise forms of this kernel measured slower).
 __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
+    if (vc_idle(ctl, tab.n, vc)) return;
     FOR_TILES(tab)
     if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
@@ -681,6 +693,7 @@ __host__ __device__ inline long long prolong_box(const Lvl& F, const Lvl& C) {
 }
 
 __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
+    if (vc_idle(ctl, tab.n, vc)) return;
     FOR_TILES(tab)
     if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
@@ -774,6 +787,7 @@ struct PairTile {
 template <int LANES>
 __global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANES>::THREADS)
     kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir, int vc) {
+    if (vc_idle(ctl, tab.n, vc)) return;
     using T = PairTile<LANES>;
     __shared__ float red[kPairHZ][kPairHY][T::RX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -856,13 +870,18 @@ __global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANE
 // a Neumann problem is solvable only for zero-mean data -- red-black sweeps
 // from zero, the mean of e removed), then prolongation and post-smoothing
 // back up.  Sums use a fixed tree.  Replaces one launch per level and sweep.
+// One colour: the threads walk that colour's cells only, (nx+1)/2 slots per
+// (y, z) row (the last one past the row when the row's colour count is
+// smaller), so a sweep costs half the index decoding of a walk over all cells.
 __device__ void sm_smooth(const Lvl& L, float* e, const float* r, int color) {
-    const int n = L.nx * L.ny * L.nz, nxy = L.nx * L.ny;
+    const int hx = (L.nx + 1) / 2, m = hx * L.ny * L.nz, nxy = L.nx * L.ny;
     const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const unsigned q = L.fnx.div((unsigned)i), zz = L.fny.div(q);
-        const int x = i - (int)q * L.nx, y = (int)q - (int)zz * L.ny, z = (int)zz;
-        if (((x + y + z) & 1) != color) continue;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        const unsigned q = L.fhx.div((unsigned)j), zz = L.fny.div(q);
+        const int y = (int)q - (int)zz * L.ny, z = (int)zz;
+        const int x = (((y + z) & 1) != color ? 1 : 0) + 2 * (j - (int)q * hx);
+        if (x >= L.nx) continue;
+        const int i = x + L.nx * (int)q;
         const float c = e[i];
         const float sx = (x > 0 ? e[i - 1] : c) + (x < L.nx - 1 ? e[i + 1] : c);
         const float sy = (y > 0 ? e[i - L.nx] : c) + (y < L.ny - 1 ? e[i + L.nx] : c);
@@ -884,6 +903,7 @@ __device__ __forceinline__ float sm_res(const Lvl& L, const float* e, const floa
 
 __global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, const Ctl* ctl, Tab tab, int nu,
                                                            int vc) {
+    if (vc_idle(ctl, tab.n, vc)) return;
     extern __shared__ float tsm[];
     __shared__ float red[32];
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
@@ -1519,13 +1539,13 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
         (rc = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking)) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_inst, sizeof(InstDev) * capacity)) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_st, sizeof(Status) * capacity)) != cudaSuccess ||
-        (rc = cudaMalloc(&b->d_ctl, sizeof(Ctl) * capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_ctl, sizeof(Ctl) * (capacity + 1))) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_tab, sizeof(int) * (size_t)S_COUNT * (capacity + 1))) != cudaSuccess) {
         *err = std::string("aeroflux: batch tables: ") + cudaGetErrorString(rc);
         batch_destroy(b);
         return nullptr;
     }
-    cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl) * capacity, b->stream);
+    cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl) * (capacity + 1), b->stream);
     if (pool_bytes) {
         if (!b->pool.init(pool_bytes)) {
             *err = "aeroflux: batch device pool of " + std::to_string(pool_bytes) + " bytes: out of memory";
@@ -1584,6 +1604,17 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
                 FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr,
                 FastDiv((unsigned)std::max(1, pair_wide_x(nx) / kPairWideX)),
                 FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY)), pair_wide_x(nx)};
+        // An axis of extent 1 adds nothing to L e (its Neumann neighbours are
+        // the cell itself, so its second difference is exactly 0); with its
+        // weight kept, the relaxation would count the cell's old value as
+        // two neighbours and damp every update on levels whose other axes
+        // coarsened (weights 1/4, 1/16, ...).  Its weight is 0 unless every
+        // axis has extent 1.
+        if (nx > 1 || ny > 1 || nz > 1) {
+            if (nx == 1) L.wx = 0.0f;
+            if (ny == 1) L.wy = 0.0f;
+            if (nz == 1) L.wz = 0.0f;
+        }
         const long long c = (long long)nx * ny * nz;
         const int cx = nx % 2 == 0 && nx >= 4, cy = ny % 2 == 0 && ny >= 4, cz = nz % 2 == 0 && nz >= 4;
         if (c <= kCoarsestCells || !(cx || cy || cz) || n == kMaxLev) break;
