@@ -111,6 +111,7 @@ struct InstDev {
     FastDiv fnx, fny;        // NX, NY
     float* sh[3];            // binary32 shadow of the current U, V, W (the sweeps' taps)
     int warm;                // 1: a projection starts from the last pressure, 0: from zero
+    int bc_off[10];          // velocity BC write sets: prefix of the nine (component, set) counts
     Lvl lev[kMaxLev];
 };
 
@@ -196,21 +197,17 @@ __global__ void kb_bc(const InstDev* inst, Status* st, Tab tab, int parity, int 
     double* u = cur(I, 1, parity);
     double* v = cur(I, 2, parity);
     double* w = cur(I, 3, parity);
-    const long long n = bc_count(I.g);
+    const int n = I.bc_off[9];
     FOR_ELEMS(tab)
     if (el >= n) break;
-    long long i = el;
-    int comp = 0, set = 0;
-    for (;;) {
-        const BcComp c = bc_comp(I.g, comp, u, v, w);
-        const long long cnt = bc_set_count(c, set);
-        if (i < cnt) {
-            bc_cell(c, I.g.G, set, i);
-            break;
-        }
-        i -= cnt;
-        if (++set == 3) { set = 0; ++comp; }
-    }
+    // Write set k = 3 * component + set holds elements bc_off[k] ..
+    // bc_off[k+1]-1 (bc_set_count in that order).
+    const int e = (int)el;
+    int k = 0;
+#pragma unroll
+    for (int j = 1; j < 9; ++j) k += e >= I.bc_off[j] ? 1 : 0;
+    const int comp = k / 3;
+    bc_cell(bc_comp(I.g, comp, u, v, w), I.g.G, k - 3 * comp, e - I.bc_off[k]);
     END_ELEMS
     END_TILES
 }
@@ -1728,6 +1725,19 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.ffz = FastDiv((unsigned)(I.g.NZ + 1));
     I.fnx = FastDiv((unsigned)I.g.NX);
     I.fny = FastDiv((unsigned)I.g.NY);
+    {
+        // bc_set_count of each (component, set), component-major: extents
+        // (normal, first tangential, second tangential) per component.
+        const long long N[3][3] = {{I.g.NX, I.g.NY, I.g.NZ}, {I.g.NY, I.g.NX, I.g.NZ}, {I.g.NZ, I.g.NX, I.g.NY}};
+        long long acc = 0;
+        for (int c = 0; c < 3; ++c)
+            for (int set = 0; set < 3; ++set) {
+                I.bc_off[3 * c + set] = (int)acc;
+                const long long Nn = N[c][0], N1 = N[c][1], N2 = N[c][2];
+                acc += set == 0 ? 2 * N1 * N2 : (set == 1 ? 2 * (Nn + 1) * N2 : 2 * (Nn + 1) * (N1 + 2));
+            }
+        I.bc_off[9] = (int)acc;
+    }
     I.nlev = plan_levels(I.g.NX, I.g.NY, I.g.NZ, I.lev, &I.coarse_sweeps);
     I.tail = plan_tail(I.lev, I.nlev, &I.tail_floats, b->per_level);
     const int lim = I.tail >= 0 ? I.tail : I.nlev - 1;
