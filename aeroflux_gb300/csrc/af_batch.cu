@@ -1171,14 +1171,14 @@ unsigned big_coarse_levels(const Batch* b) {
     return m;
 }
 
-// Levels some slot smooths with fused pairs (pair = true) or in place.
-unsigned smooth_levels(const Batch* b, bool pair) {
+// Levels some slot smooths in place (in-place colour sweeps, no second buffer).
+unsigned single_levels(const Batch* b) {
     unsigned m = 0;
     for (const auto& s : b->slots) {
         if (!s.used) continue;
         const int lim = s.d.tail >= 0 ? s.d.tail : s.d.nlev - 1;
         for (int l = 0; l < lim; ++l)
-            if ((s.d.lev[l].e2 != nullptr) == pair) m |= 1u << l;
+            if (!s.d.lev[l].e2) m |= 1u << l;
     }
     return m;
 }
@@ -1468,7 +1468,7 @@ cudaError_t prepare(Batch* b) {
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     const int L = max_levels(b);
     const unsigned big = big_coarse_levels(b), pair = pair_levels(b, false), pairn = pair_levels(b, true),
-                   single = smooth_levels(b, false);
+                   single = single_levels(b);
     const size_t tsm = tail_smem_bytes(b);
     if (b->graph && (L > b->graph_levels || (big & ~b->graph_big) || (pair & ~b->graph_pair) ||
                      (pairn & ~b->graph_pairn) || (single & ~b->graph_single) || tsm > b->tail_smem ||
@@ -1876,7 +1876,7 @@ cudaError_t batch_prepare_capture(Batch* b) {
     b->graph_big |= big_coarse_levels(b);
     b->graph_pair |= pair_levels(b, false);
     b->graph_pairn |= pair_levels(b, true);
-    b->graph_single |= smooth_levels(b, false);
+    b->graph_single |= single_levels(b);
     b->tail_smem = std::max(b->tail_smem, tail_smem_bytes(b));
     if ((rc = cudaFuncSetAttribute(kb_vtail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem)) !=
         cudaSuccess)
