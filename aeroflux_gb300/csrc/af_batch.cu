@@ -311,7 +311,7 @@ __device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* 
     dd += rb;
     const int s = AX == 0 ? 1 : (AX == 1 ? (int)d.sy : (int)d.sz);
     const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
-    // Face velocity taps (mx_face_vel): offsets from (x, y, z) in the axis
+    // Face velocity taps (summed by mx_face_vel4): offsets from (x, y, z) in the axis
     // component, in the order they are summed.
     const float* __restrict__ va = I.sh[AX] + (long long)y * a.sy + (long long)z * a.sz;
     const int ay = (int)a.sy, az = (int)a.sz;
