@@ -302,7 +302,7 @@ __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
 // of mx_face_update and one store.
 template <int AX, int C>
 __device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* __restrict__ dd, int y, int z,
-                                          int lane, int phase) {
+                                          int x0, int x1, int phase) {
     const Geom& g = I.g;
     const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
     const Dims& a = AX == 0 ? g.u : (AX == 1 ? g.v : g.w);
@@ -322,7 +322,6 @@ __device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* 
     if (C == 1 && AX == 2) { o0 = -ay; o1 = 0; o2 = az - ay; o3 = az; }
     if (C == 2 && AX == 0) { o0 = -az; o1 = 1 - az; o2 = 0; o3 = 1; }
     if (C == 2 && AX == 1) { o0 = -az; o1 = ay - az; o2 = 0; o3 = ay; }
-    const int x0 = g.G + lane, x1 = g.G + g.NX + (C == 0);
     const float dt_invh = I.dt_invh, lam = I.lam;
     auto vel_at = [&](int x) {
         return C == AX ? src[x] : mx_face_vel4(va[x + o0], va[x + o1], va[x + o2], va[x + o3]);
@@ -344,24 +343,42 @@ __device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* 
     }
 }
 
+// Iteration space of the sweep: 32 lanes per face row of the three
+// components, then the U rows' last faces (x = G + NX), 32 rows to a warp:
+// a U row has NX + 1 faces, and with NX a multiple of 32 its last face would
+// otherwise cost a whole warp iteration of one lane.
+__host__ __device__ inline long long sweep_box(const Geom& g) {
+    return 32ll * (3ll * (g.NY + 1) * (g.NZ + 1) + ((long long)g.NY * g.NZ + 31) / 32);
+}
+
 template <int AX>
 __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, int phase) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (gated(&st[s], phase)) continue;
     const Geom& g = I.g;
-    const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1);
+    const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1), n = sweep_box(g);
     FOR_ELEMS(tab)
+    if (el >= n) break;
     const long long row = el >> 5;
-    if (row >= rows) break;
     const int lane = (int)(el & 31);
+    if (row >= rows) {
+        // Last U face of U row q.
+        const long long q = (row - rows) * 32 + lane;
+        if (q >= (long long)g.NY * g.NZ) continue;
+        const unsigned zz = I.fny.div((unsigned)q);
+        const int y = g.G + (int)((unsigned)q - zz * (unsigned)g.NY), z = g.G + (int)zz;
+        sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, g.G + g.NX, g.G + g.NX + 1, phase);
+        continue;
+    }
     const unsigned r = (unsigned)row, r2 = I.ffy.div(r), cc = I.ffz.div(r2);
     const int c = (int)cc;
     const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
     if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
-    if (c == 0) sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, lane, phase);
-    else if (c == 1) sweep_row<AX, 1>(I, st + s, cur(I, 6, parity), y, z, lane, phase);
-    else sweep_row<AX, 2>(I, st + s, cur(I, 7, parity), y, z, lane, phase);
+    const int x0 = g.G + lane, x1 = g.G + g.NX;  // the U rows' last faces come after the rows
+    if (c == 0) sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, x0, x1, phase);
+    else if (c == 1) sweep_row<AX, 1>(I, st + s, cur(I, 6, parity), y, z, x0, x1, phase);
+    else sweep_row<AX, 2>(I, st + s, cur(I, 7, parity), y, z, x0, x1, phase);
     END_ELEMS
     END_TILES
 }
@@ -1211,7 +1228,8 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     const long long per = (long long)sh.tpb * sh.ept;
     long long n = 0;
     if (st == S_BC) n = bc_count(I.g);
-    else if (st == S_SWEEP || st == S_GRAD) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
+    else if (st == S_SWEEP) n = sweep_box(I.g);
+    else if (st == S_GRAD) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
     else if (st == S_SHADOW) n = quads(I.g.u.count) + quads(I.g.v.count) + quads(I.g.w.count);
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
