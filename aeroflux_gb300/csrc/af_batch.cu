@@ -1671,6 +1671,27 @@ Dims dims_of(const af_field_desc& d) {
 
 }  // namespace
 
+bool batch_config_fits(const af_config& c, std::string* err) {
+    const int64_t g = c.ghost, cx = c.nx + 2 * g, cy = c.ny + 2 * g, cz = c.nz + 2 * g;
+    // The kernels decode 32-bit element numbers (FastDiv) and keep the nine
+    // velocity-BC write sets' prefix in int (InstDev::bc_off).
+    Geom G{};
+    G.NX = (int)std::min<int64_t>(c.nx, INT32_MAX);
+    G.NY = (int)std::min<int64_t>(c.ny, INT32_MAX);
+    G.NZ = (int)std::min<int64_t>(c.nz, INT32_MAX);
+    const bool dims_ok = c.nx < (1 << 30) && c.ny < (1 << 30) && c.nz < (1 << 30) && g < (1 << 20);
+    const double big = 2147483648.0;  // 2^31, compared in double so no product overflows
+    const bool fields_ok = (double)(cx + 1) * cy * cz < big && (double)cx * (cy + 1) * cz < big &&
+                           (double)cx * cy * (cz + 1) < big;
+    if (!dims_ok || !fields_ok || (double)face_box(G) >= 2.0 * big || (double)bc_count(G) >= big) {
+        if (err)
+            *err = "aeroflux: grid too large for one batch slot (2^31 elements per field and per velocity-BC "
+                   "write set)";
+        return false;
+    }
+    return true;
+}
+
 size_t batch_slot_bytes(const af_config& c) {
     int64_t off = 0;
     const int64_t g = c.ghost, cx = c.nx + 2 * g, cy = c.ny + 2 * g, cz = c.nz + 2 * g;
@@ -1730,9 +1751,7 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     I.g.u = dims_of(S.desc[1]);
     I.g.v = dims_of(S.desc[2]);
     I.g.w = dims_of(S.desc[3]);
-    if (face_box(I.g) >= (1ll << 32) || S.desc[1].count >= (1ll << 31) || S.desc[2].count >= (1ll << 31) ||
-        S.desc[3].count >= (1ll << 31)) {
-        *err = "aeroflux: grid too large for one batch slot (2^31 elements per field)";
+    if (!batch_config_fits(c, err)) {
         S = SlotHost();
         return -1;
     }

@@ -22,6 +22,10 @@ void batch_destroy(Batch* b);
 
 // Bytes of device memory one slot needs for a normalized MIXED config.
 size_t batch_slot_bytes(const af_config& c);
+// Whether a normalized config fits the 32-bit index arithmetic of a slot
+// (face box < 2^32, each field and the velocity-BC write set < 2^31
+// elements); otherwise false with the message in *err.  Host only.
+bool batch_config_fits(const af_config& c, std::string* err);
 
 // Puts a normalized MIXED config into a free slot.  `arena`, when non-NULL,
 // is external field memory in the reference layout (the single-grid engine);

@@ -1077,6 +1077,7 @@ int af_batch_slot_bytes(const af_config* cfg, int64_t* bytes) {
     if (!cfg || !bytes) return AF_ERR_ARG;
     af_config c = *cfg;
     if (!normalize(&c).empty()) return AF_ERR_CONFIG;
+    if (!af::batch_config_fits(c, nullptr)) return AF_ERR_CONFIG;
     *bytes = (int64_t)af::batch_slot_bytes(c);
     return AF_OK;
 }

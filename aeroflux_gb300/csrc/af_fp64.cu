@@ -830,12 +830,15 @@ extern "C" int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, 
         put(err, errlen, "aeroflux: kinetic energy without allocation: extents, ghost and h must be positive");
         return AF_ERR_ARG;
     }
-    if (cfg->nz > kNoAllocMaxPlanes || cfg->nx >= (1 << 20) || cfg->ny >= (1 << 20)) {
+    // The kernels index planes and rows in int: extents and the ghost stay
+    // below 2^20 so every padded coordinate fits.
+    if (cfg->nz > kNoAllocMaxPlanes || cfg->nx >= (1 << 20) || cfg->ny >= (1 << 20) || cfg->ghost >= (1 << 20)) {
         char m[256];
         snprintf(m, sizeof m,
-                 "aeroflux: kinetic energy without allocation supports at most %d z-planes (and nx, ny < 2^20), "
-                 "got %lldx%lldx%lld",
-                 kNoAllocMaxPlanes, (long long)cfg->nx, (long long)cfg->ny, (long long)cfg->nz);
+                 "aeroflux: kinetic energy without allocation supports at most %d z-planes (and nx, ny, ghost "
+                 "< 2^20), got %lldx%lldx%lld ghost %lld",
+                 kNoAllocMaxPlanes, (long long)cfg->nx, (long long)cfg->ny, (long long)cfg->nz,
+                 (long long)cfg->ghost);
         put(err, errlen, m);
         return AF_ERR_ARG;
     }

@@ -12,8 +12,9 @@ reference's Mcell/s of bench_test.go:32).
 ours: `value` is device time (CUDA event nodes carried by the step graph on
 the engine's stream) over exactly K steps with the field resident in HBM; the
 working set (1.1 GB per grid) is far larger than L2.  `e2e` times the same
-step through the C ABI with the field uploaded from pinned host memory and
-the step's result (MaxDivergence) read back, every step.  `roofline` is the
+step through the C ABI as a Mesh.Data caller sees it: U, V, W uploaded from
+pinned host memory, Step, MaxDivergence read back and U, V, W downloaded,
+every step.  `roofline` is the
 red-black sweep kernel, the dominant one.  `cpu_baseline` times the CPU
 oracle (a C restatement of the reference's Go CPU path) on a bounded sample.
 
@@ -162,17 +163,13 @@ def base_config():
 
 
 def run_oracle_steps(warmup: int, steps: int, threads: int):
-    """The CPU path (oracle) on the same workload: seconds per step."""
-    from aeroflux_gb300 import Config
-    from aeroflux_gb300.workloads import taylor_green
+    """The CPU path (oracle) on the same workload: seconds per step.  The
+    input is seeded by the oracle itself (the same Taylor-Green + PCG32
+    field), so this path maps no product code."""
     from oracle.oracle import OracleEngine
-    cfg = Config(NX=N, NY=N, NZ=N, H=1.0 / N, DT=DT, Viscosity=NU, Density=1.0, GaussSeidelIters=GSI)
-    u, v, w = taylor_green(cfg, 1.0, NOISE, 42, 0)
     with OracleEngine(nx=N, ny=N, nz=N, h=1.0 / N, dt=DT, viscosity=NU, density=1.0,
                       gauss_seidel_iters=GSI, workers=threads) as o:
-        o.data(1)[:] = u
-        o.data(2)[:] = v
-        o.data(3)[:] = w
+        o.seed_taylor_green(1.0, NOISE, 42, 0)
         o.apply_velocity_bc()
         for _ in range(warmup):
             o.step()
@@ -194,16 +191,27 @@ def common_fields(args, world):
     }
 
 
+def product_library_mapped() -> bool:
+    """Whether this process has mapped the product's CUDA library."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libaeroflux_cuda" in line for line in f)
+    except OSError:
+        return False
+
+
 def bench_reference(args):
     rank, _, world = rank_info()
     if rank != 0:
         return 0
     threads = cpu_threads()
     sec = run_oracle_steps(args.warmup, args.steps, threads)
+    if product_library_mapped():
+        raise RuntimeError("the reference arm mapped the product library")
     val = N ** 3 / sec
     line = common_fields(args, world)
     line.update({
-        "impl": "reference", "value": val, "ms_per_step": sec * 1e3,
+        "impl": "reference", "value": val, "ms_per_step": sec * 1e3, "product_library_mapped": False,
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.warmup} warm-up + {args.steps} timed Steps of the {N}^3 workload, "
                                    f"C restatement of the Go CPU path, {threads} worker threads"},
@@ -391,22 +399,30 @@ def bench_ours(args):
         pin = torch.cuda.is_available()
     except ImportError:
         pin = False
-    host = []
+    host, back = [], []
     for a in (u, v, w):
         if pin:
             tt = torch.from_numpy(a).pin_memory()
             host.append((tt, tt.data_ptr(), a.size))
+            bb = torch.empty(a.size, dtype=torch.float64).pin_memory()
+            back.append((bb, bb.data_ptr(), a.size))
         else:
+            bb = a.copy()
             host.append((a, a.ctypes.data, a.size))
+            back.append((bb, bb.ctypes.data, a.size))
     lib = L.lib()
     out = C.c_double()
     e2e_steps = max(3, args.steps // 2)
 
     def e2e_step():
+        # The drop-in's Mesh.Data mirror: push the caller's fields, Step,
+        # pull the fields back, and read the step's MaxDivergence.
         for fid, (_, ptr, n) in zip((1, 2, 3), host):
             e._check(lib.af_field_upload(e._h, fid, ptr, n))
         e._check(lib.af_step(e._h, 1))
         e._check(lib.af_max_divergence(e._h, C.byref(out)))
+        for fid, (_, ptr, n) in zip((1, 2, 3), back):
+            e._check(lib.af_field_download(e._h, fid, ptr, n))
 
     e2e_step()  # warm-up (graph rebuild without event nodes)
     dist.barrier()
@@ -477,8 +493,9 @@ def bench_ours(args):
     line.update({
         "value": value, "ms_per_step": t["dev_s"] * 1e3 / args.steps, "wall_ms_per_step": t["wall_s"] * 1e3 / args.steps,
         "gpu_launches": t["launches"] * args.steps,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8,
-                "steps": e2e_steps, "host_memory": "pinned" if pin else "pageable"},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
+                "steps": e2e_steps, "host_memory": "pinned" if pin else "pageable",
+                "per_step": "upload U, V, W; Step; MaxDivergence; download U, V, W (the Mesh.Data mirror)"},
         "roofline": {"bound": "hbm", "kernel": "k_rbgs_fp64 (one colour sweep)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                      "traffic": traffic, "launch_us": rb_launch_s * 1e6,

@@ -355,12 +355,14 @@ int af_seed_taylor_green(const af_config* cfg, double amp, double noise, uint64_
  * unused) on the current device; the sum is the fixed-order tree of
  * af_kinetic_energy.  Its scratch is a static 128 KiB device array held by
  * every GPU that loads the library until exit, so nz is limited to 16384
- * z-planes (larger grids are rejected with AF_ERR_ARG and a message in err).
- * The first call on a device resolves the array's address there; make that
- * first call before any stream capture.  Enqueues on `stream` (a
- * cudaStream_t, NULL for the default stream) and blocks until *out (host)
- * holds the result.  All calls share the one array: calls that overlap on
- * the GPU race. */
+ * z-planes, and nx, ny and ghost to below 2^20 (larger grids are rejected
+ * with AF_ERR_ARG and a message in err).  The first call on a device
+ * resolves the array's address there (a one-time set-up); make that first
+ * call before any stream capture.  The call is synchronous: it enqueues on
+ * `stream` (a cudaStream_t, NULL for the default stream), waits for that
+ * stream and copies the result to *out (host), so it must not be made while
+ * `stream` is being captured.  All calls share the one array: calls that
+ * overlap on the GPU race. */
 int af_kinetic_energy_noalloc(const af_config* cfg, const double* u, const double* v, const double* w,
                               void* stream, double* out, char* err, size_t errlen);
 

@@ -809,6 +809,60 @@ void orc_seed_vortex(orc_engine* e, double amp) {
     orc_apply_velocity_bc(e);
 }
 
+/* PCG32, XSH-RR 64/32 (O'Neill 2014), pcg32_srandom_r seeding; a 53-bit
+ * uniform double in [0, 1) from two outputs. */
+typedef struct { uint64_t state, inc; } orc_pcg32;
+static uint32_t orc_pcg_next(orc_pcg32* r) {
+    uint64_t old = r->state;
+    r->state = old * 6364136223846793005ull + r->inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+static double orc_pcg_uniform(orc_pcg32* r) {
+    uint32_t a = orc_pcg_next(r) >> 5, b = orc_pcg_next(r) >> 6;
+    return ((double)a * 67108864.0 + (double)b) * (1.0 / 9007199254740992.0);
+}
+
+/* The benchmark's synthetic field: Taylor-Green of amplitude amp at the
+ * staggered face positions plus uniform [-noise, noise] noise, over
+ * seedVortex's index ranges (engine_test.go:313-333) in U, V, W and z, y, x
+ * order.  U, V, W are zeroed first; no BC is applied. */
+void orc_seed_taylor_green(orc_engine* e, double amp, double noise, uint64_t seed, uint64_t stream) {
+    int64_t g = e->G;
+    const orc_field* fu = &e->f[ORC_U];
+    const orc_field* fv = &e->f[ORC_V];
+    const orc_field* fw = &e->f[ORC_W];
+    double* u = D(e, ORC_U);
+    double* v = D(e, ORC_V);
+    double* w = D(e, ORC_W);
+    memset(u, 0, sizeof(double) * (size_t)fu->count);
+    memset(v, 0, sizeof(double) * (size_t)fv->count);
+    memset(w, 0, sizeof(double) * (size_t)fw->count);
+    double h = e->cfg.h, twopi = 6.283185307179586;
+    orc_pcg32 r = {0u, (stream << 1u) | 1u};
+    orc_pcg_next(&r);
+    r.state += seed;
+    orc_pcg_next(&r);
+    for (int64_t z = g; z < g + e->NZ; ++z)
+        for (int64_t y = g; y < g + e->NY; ++y)
+            for (int64_t x = g; x <= g + e->NX; ++x) {
+                double X = (double)(x - g) * h, Y = ((double)(y - g) + 0.5) * h, Z = ((double)(z - g) + 0.5) * h;
+                u[IX(fu, x, y, z)] = amp * sin(twopi * X) * cos(twopi * Y) * cos(twopi * Z) +
+                                     noise * (2.0 * orc_pcg_uniform(&r) - 1.0);
+            }
+    for (int64_t z = g; z < g + e->NZ; ++z)
+        for (int64_t y = g; y <= g + e->NY; ++y)
+            for (int64_t x = g; x < g + e->NX; ++x) {
+                double X = ((double)(x - g) + 0.5) * h, Y = (double)(y - g) * h, Z = ((double)(z - g) + 0.5) * h;
+                v[IX(fv, x, y, z)] = -amp * cos(twopi * X) * sin(twopi * Y) * cos(twopi * Z) +
+                                     noise * (2.0 * orc_pcg_uniform(&r) - 1.0);
+            }
+    for (int64_t z = g; z <= g + e->NZ; ++z)
+        for (int64_t y = g; y < g + e->NY; ++y)
+            for (int64_t x = g; x < g + e->NX; ++x) w[IX(fw, x, y, z)] = 0.0 + noise * (2.0 * orc_pcg_uniform(&r) - 1.0);
+}
+
 /* Example's shear layer, example_test.go:34-47 (no BC: Step applies it). */
 void orc_seed_shear_layer(orc_engine* e) {
     int64_t g = e->G;

@@ -87,6 +87,8 @@ double orc_cfl(orc_engine* e);             /* stencil.go:336-338 */
 /* The reference's test inputs. */
 void orc_seed_vortex(orc_engine* e, double amp);  /* engine_test.go:302-335 */
 void orc_seed_shear_layer(orc_engine* e);         /* example_test.go:34-47 */
+/* The benchmark's seeded Taylor-Green + PCG32 field (no BC applied). */
+void orc_seed_taylor_green(orc_engine* e, double amp, double noise, uint64_t seed, uint64_t stream);
 
 /* Go strconv.FormatFloat(v, 'g', -1, 64), i.e. fmt's %v / %g for float64. */
 void orc_go_format_float(double v, char* out, size_t outlen);

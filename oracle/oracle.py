@@ -86,6 +86,8 @@ def lib():
             getattr(L, name).restype = C.c_double
         L.orc_seed_vortex.argtypes = [E, C.c_double]
         L.orc_seed_vortex.restype = None
+        L.orc_seed_taylor_green.argtypes = [E, C.c_double, C.c_double, C.c_uint64, C.c_uint64]
+        L.orc_seed_taylor_green.restype = None
         L.orc_go_format_float.argtypes = [C.c_double, C.c_char_p, C.c_size_t]
         L.orc_go_format_float.restype = None
         _lib = L
@@ -219,6 +221,9 @@ class OracleEngine:
 
     def seed_vortex(self, amp: float = 1.0):
         lib().orc_seed_vortex(self._h, amp)
+
+    def seed_taylor_green(self, amp: float = 1.0, noise: float = 0.01, seed: int = 42, stream: int = 0):
+        lib().orc_seed_taylor_green(self._h, amp, noise, seed, stream)
 
     def seed_shear_layer(self):
         lib().orc_seed_shear_layer(self._h)

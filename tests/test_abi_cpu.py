@@ -165,3 +165,31 @@ def test_create_without_device_fails_cleanly():
     rc = L.lib().af_create(C.byref(c), C.byref(h), buf, 512)
     assert rc in (L.AF_ERR_CUDA, L.AF_ERR_NOMEM) and not h.value
     assert buf.value.decode().startswith("aeroflux: ")
+
+
+def test_batch_slot_rejects_grids_beyond_its_32_bit_index_space():
+    """A thin wide grid whose fields fit 2^31 elements but whose velocity-BC
+    write set does not (about 2.4e9 ghost cells at 20000x20000x1) is refused
+    before any device work, as is a field beyond 2^31 elements."""
+    from aeroflux_gb300 import _lib as LL
+    from aeroflux_gb300.batch import Batch
+    ok = Config(NX=64, NY=48, NZ=32, H=1 / 64, DT=0.001, Precision=LL.AF_PRECISION_MIXED)
+    assert Batch.slot_bytes(ok) > 0
+    for dims in ((20000, 20000, 1), (1300, 1300, 1300)):
+        c = Config(NX=dims[0], NY=dims[1], NZ=dims[2], H=1 / max(dims), DT=1e-9, Viscosity=1e-5,
+                   Precision=LL.AF_PRECISION_MIXED)
+        with pytest.raises(AerofluxError):
+            Batch.slot_bytes(c)
+
+
+def test_oracle_seeder_matches_the_product_generator():
+    """The reference arm of the benchmark seeds through the oracle alone; its
+    field is the product generator's bit for bit (same host libm)."""
+    from oracle.oracle import OracleEngine
+    cfg = Config(NX=9, NY=7, NZ=5, H=1 / 9, DT=0.001)
+    cfg.Normalize()
+    u, v, w = taylor_green(cfg, 1.0, 0.01, seed=42, stream=2)
+    with OracleEngine(nx=9, ny=7, nz=5, h=1 / 9, dt=0.001, viscosity=0.0, density=1.0) as o:
+        o.seed_taylor_green(1.0, 0.01, 42, 2)
+        for fid, a in ((1, u), (2, v), (3, w)):
+            assert np.array_equal(o.data(fid).view(np.uint64), a.view(np.uint64))
