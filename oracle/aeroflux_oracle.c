@@ -260,6 +260,10 @@ int64_t orc_mac_bytes(int64_t nx, int64_t ny, int64_t nz, int64_t ghost) {
     return mac_layout(nx, ny, nz, ghost, f);
 }
 
+/* Planted mistakes for the oracle's self-checks (0: none); see the header. */
+static int g_orc_mut = 0;
+void orc_set_mutation(int m) { g_orc_mut = m; }
+
 static inline double* D(orc_engine* e, int id) { return (double*)(e->arena + e->f[id].off); }
 static inline int64_t IX(const orc_field* f, int64_t x, int64_t y, int64_t z) { return x + y * f->sy + z * f->sz; }
 
@@ -413,6 +417,12 @@ static inline int sample_trilinear(const orc_field* f, const double* d, double p
     double c10 = d[i010] * (1 - tx) + d[i110] * tx;
     double c01 = d[i001] * (1 - tx) + d[i101] * tx;
     double c11 = d[i011] * (1 - tx) + d[i111] * tx;
+    if (g_orc_mut == 2) { /* a contracting compiler's x * y + z */
+        c00 = fma(d[i100], tx, d[i000] * (1 - tx));
+        c10 = fma(d[i110], tx, d[i010] * (1 - tx));
+        c01 = fma(d[i101], tx, d[i001] * (1 - tx));
+        c11 = fma(d[i111], tx, d[i011] * (1 - tx));
+    }
     double c0 = c00 * (1 - ty) + c10 * ty;
     double c1 = c01 * (1 - ty) + c11 * ty;
     *out = c0 * (1 - tz) + c1 * tz;
@@ -489,6 +499,8 @@ static void commit_velocity(orc_engine* e) {
     t = e->f[ORC_W]; e->f[ORC_W] = e->f[ORC_TMP2]; e->f[ORC_TMP2] = t;
 }
 
+void orc_commit_velocity(orc_engine* e) { commit_velocity(e); }
+
 /* applyVelocityBC, stencil.go:246-315 (serial, in the reference's loop order). */
 void orc_apply_velocity_bc(orc_engine* e) {
     int64_t g = e->G;
@@ -517,16 +529,22 @@ void orc_apply_velocity_bc(orc_engine* e) {
             w[IX(fw, x, y, z0)] = 0;
             w[IX(fw, x, y, z1)] = 0;
         }
-    for (int64_t z = z0; z < z1; ++z)
-        for (int64_t x = ux0; x <= ux1; ++x) {
-            u[IX(fu, x, y0 - 1, z)] = -u[IX(fu, x, y0, z)];
-            u[IX(fu, x, y1, z)] = -u[IX(fu, x, y1 - 1, z)];
+    for (int pass = 0; pass < 2; ++pass) {
+        /* stencil.go:279-284 then 285-290; mutation 1 swaps them. */
+        if ((pass == 0) == (g_orc_mut != 1)) {
+            for (int64_t z = z0; z < z1; ++z)
+                for (int64_t x = ux0; x <= ux1; ++x) {
+                    u[IX(fu, x, y0 - 1, z)] = -u[IX(fu, x, y0, z)];
+                    u[IX(fu, x, y1, z)] = -u[IX(fu, x, y1 - 1, z)];
+                }
+        } else {
+            for (int64_t y = y0 - 1; y <= y1; ++y)
+                for (int64_t x = ux0; x <= ux1; ++x) {
+                    u[IX(fu, x, y, z0 - 1)] = -u[IX(fu, x, y, z0)];
+                    u[IX(fu, x, y, z1)] = -u[IX(fu, x, y, z1 - 1)];
+                }
         }
-    for (int64_t y = y0 - 1; y <= y1; ++y)
-        for (int64_t x = ux0; x <= ux1; ++x) {
-            u[IX(fu, x, y, z0 - 1)] = -u[IX(fu, x, y, z0)];
-            u[IX(fu, x, y, z1)] = -u[IX(fu, x, y, z1 - 1)];
-        }
+    }
     for (int64_t z = z0; z < z1; ++z)
         for (int64_t y = y0; y <= y1; ++y) {
             v[IX(fv, g - 1, y, z)] = -v[IX(fv, g, y, z)];
@@ -596,6 +614,7 @@ static int gs_fn(orc_engine* e, const shard* s, char* msg, size_t msglen) {
             for (int64_t x = start; x < g + e->NX; x += 2) {
                 int64_t i = base + x;
                 double sum = p[i - 1] + p[i + 1] + p[i - sy] + p[i + sy] + p[i - sz] + p[i + sz];
+                if (g_orc_mut == 5) sum = (p[i - 1] + p[i + 1]) + (p[i - sy] + p[i + sy]) + (p[i - sz] + p[i + sz]);
                 p[i] = (sum - h2 * dv[IX(fd, x, y, z)]) / 6.0;
             }
         }
@@ -608,6 +627,12 @@ void orc_apply_pressure_bc(orc_engine* e) {
     double* p = D(e, ORC_P);
     int64_t g = e->G;
     int64_t x1 = g + e->NX, y1 = g + e->NY, z1 = g + e->NZ;
+    if (g_orc_mut == 4) /* z-ghosts first: edges and corners read stale ghosts */
+        for (int64_t y = g - 1; y <= y1; ++y)
+            for (int64_t x = g - 1; x <= x1; ++x) {
+                p[IX(fp, x, y, g - 1)] = p[IX(fp, x, y, g)];
+                p[IX(fp, x, y, z1)] = p[IX(fp, x, y, z1 - 1)];
+            }
     for (int64_t z = g; z < z1; ++z)
         for (int64_t y = g; y < y1; ++y) {
             p[IX(fp, g - 1, y, z)] = p[IX(fp, g, y, z)];
@@ -618,6 +643,7 @@ void orc_apply_pressure_bc(orc_engine* e) {
             p[IX(fp, x, g - 1, z)] = p[IX(fp, x, g, z)];
             p[IX(fp, x, y1, z)] = p[IX(fp, x, y1 - 1, z)];
         }
+    if (g_orc_mut == 4) return;
     for (int64_t y = g - 1; y <= y1; ++y)
         for (int64_t x = g - 1; x <= x1; ++x) {
             p[IX(fp, x, y, g - 1)] = p[IX(fp, x, y, g)];
@@ -632,10 +658,10 @@ void orc_solve_pressure_red_black(orc_engine* e) {
     for (int64_t i = 0; i < n; ++i) p[i] = 0;
     for (int64_t it = 0; it < e->cfg.gauss_seidel_iters; ++it) {
         orc_apply_pressure_bc(e);
-        e->cur_color = COLOR_RED;
+        e->cur_color = g_orc_mut == 3 ? COLOR_BLACK : COLOR_RED;
         dispatch(e, gs_fn, NULL, 0);
         orc_apply_pressure_bc(e);
-        e->cur_color = COLOR_BLACK;
+        e->cur_color = g_orc_mut == 3 ? COLOR_RED : COLOR_BLACK;
         dispatch(e, gs_fn, NULL, 0);
     }
     orc_apply_pressure_bc(e);

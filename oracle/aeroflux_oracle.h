@@ -77,6 +77,7 @@ void orc_compute_divergence(orc_engine* e);                /* project.go:42-62 *
 void orc_solve_pressure_red_black(orc_engine* e);          /* project.go:73-100 */
 void orc_apply_pressure_bc(orc_engine* e);                 /* project.go:139-163 */
 void orc_subtract_gradient(orc_engine* e);                 /* project.go:172-205 */
+void orc_commit_velocity(orc_engine* e);                   /* commitVelocity, stencil.go:230-235 */
 
 /* Diagnostics. */
 double orc_max_divergence(orc_engine* e);  /* project.go:210-232 */
@@ -89,6 +90,15 @@ void orc_seed_vortex(orc_engine* e, double amp);  /* engine_test.go:302-335 */
 void orc_seed_shear_layer(orc_engine* e);         /* example_test.go:34-47 */
 /* The benchmark's seeded Taylor-Green + PCG32 field (no BC applied). */
 void orc_seed_taylor_green(orc_engine* e, double amp, double noise, uint64_t seed, uint64_t stream);
+
+/* Planted mistakes for the oracle's self-checks (0: none): 1 runs the u
+ * z-ghost reflection (stencil.go:285-290) before the y-ghost one (279-284);
+ * 2 contracts the trilinear x-lerps into fused multiply-adds; 3 sweeps black
+ * before red (project.go:88-97); 4 mirrors the pressure z-ghosts before the
+ * x- and y-ghosts (project.go:139-163); 5 pairs the red-black neighbour sum
+ * instead of Go's left-to-right order (project.go:125).  Process-wide;
+ * tests only. */
+void orc_set_mutation(int m);
 
 /* Go strconv.FormatFloat(v, 'g', -1, 64), i.e. fmt's %v / %g for float64. */
 void orc_go_format_float(double v, char* out, size_t outlen);

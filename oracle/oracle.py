@@ -40,10 +40,18 @@ class OrcField(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("off", "nx", "ny", "nz", "sy", "sz", "count")]
 
 
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    srcs = [f for f in os.listdir(HERE) if f.endswith((".c", ".h")) or f == "Makefile"]
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in srcs)
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", HERE, "liboracle"], check=True)
+    if force or _stale():
+        subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle"], check=True)
     return LIB_PATH
 
 
@@ -86,8 +94,12 @@ def lib():
             getattr(L, name).restype = C.c_double
         L.orc_seed_vortex.argtypes = [E, C.c_double]
         L.orc_seed_vortex.restype = None
+        L.orc_commit_velocity.argtypes = [E]
+        L.orc_commit_velocity.restype = None
         L.orc_seed_taylor_green.argtypes = [E, C.c_double, C.c_double, C.c_uint64, C.c_uint64]
         L.orc_seed_taylor_green.restype = None
+        L.orc_set_mutation.argtypes = [C.c_int]
+        L.orc_set_mutation.restype = None
         L.orc_go_format_float.argtypes = [C.c_double, C.c_char_p, C.c_size_t]
         L.orc_go_format_float.restype = None
         _lib = L
@@ -192,6 +204,9 @@ class OracleEngine:
     def sweep(self, axis: int, dt: float):
         self._err_call(lib().orc_sweep, axis, dt)
 
+    def commit_velocity(self):
+        lib().orc_commit_velocity(self._h)
+
     def apply_velocity_bc(self):
         lib().orc_apply_velocity_bc(self._h)
 
@@ -227,3 +242,8 @@ class OracleEngine:
 
     def seed_shear_layer(self):
         lib().orc_seed_shear_layer(self._h)
+
+
+def set_mutation(m: int) -> None:
+    """Plant mistake m into the oracle (0: none); see aeroflux_oracle.h."""
+    lib().orc_set_mutation(m)
