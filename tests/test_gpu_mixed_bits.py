@@ -235,10 +235,12 @@ def test_device_seeded_slot_bit_exact():
 
 @pytest.mark.parametrize("mutation,n", [(1, (24, 20, 18)), (2, (24, 20, 18)), (3, (24, 20, 18)), (4, (40, 1, 1))])
 def test_mutated_mixed_oracle_is_caught(mutation, n):
-    e, o = make_mixed_pair(n)
-    e.Step(1)
+    # The mutation is in force while the restatement plans its hierarchy
+    # (mutation 4 acts there) and while it steps.
     mixed_oracle.set_mutation(mutation)
     try:
+        e, o = make_mixed_pair(n)
+        e.Step(1)
         o.step(1)
     finally:
         mixed_oracle.set_mutation(0)
