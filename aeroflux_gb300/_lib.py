@@ -127,6 +127,7 @@ SIGNATURES = {
     "af_server_results": (C.c_int, [_E, C.POINTER(AfRequestResult), C.c_int64, C.POINTER(C.c_int64)]),
     "af_server_download": (C.c_int, [_E, C.c_int64, C.c_int, C.c_void_p, C.c_size_t]),
     "af_server_release": (C.c_int, [_E, C.c_int64]),
+    "af_server_cancel_queued": (C.c_int, [_E, C.POINTER(C.c_int64)]),
     "af_server_get_stats": (C.c_int, [_E, C.POINTER(AfServerStats)]),
     "af_server_tune": (C.c_int, [_E, C.c_int32, *_ERR]),
     "af_server_destroy": (None, [_E]),

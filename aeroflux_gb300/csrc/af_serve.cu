@@ -283,6 +283,13 @@ int af_server_release(af_server* s, int64_t id) {
     return fail(s, AF_ERR_ARG, "aeroflux: no retained result with that id");
 }
 
+int af_server_cancel_queued(af_server* s, int64_t* cancelled) {
+    if (!s) return AF_ERR_ARG;
+    if (cancelled) *cancelled = (int64_t)s->queue.size();
+    s->queue.clear();
+    return AF_OK;
+}
+
 int af_server_get_stats(af_server* s, af_server_stats* out) {
     if (!s || !out) return AF_ERR_ARG;
     out->queued = (int64_t)s->queue.size();

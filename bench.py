@@ -247,6 +247,23 @@ def new_engine(precision: int, local: int, rank: int, div_tol: float = 0.0):
     return e, (u, v, w)
 
 
+def velocity_host(e):
+    return [e.download(n) for n in ("U", "V", "W")]
+
+
+def error_vs_fp64(mixed_fields, ref_engine, md_mixed: float, steps: int) -> dict:
+    """max|dU,dV,dW| / max|ref| of the mixed form against the FP64 form with
+    the multigrid projection (bit-exact FP64 sweeps, max|div| <= 1e-12),
+    both from the same field after the same Steps."""
+    out = {"reference": "FP64 form + EnableMultigridSolver(1e-12), same initial field and Steps",
+           "steps": steps, "max_divergence_mixed": md_mixed, "max_divergence_fp64": ref_engine.MaxDivergence()}
+    for name, a in zip(("U", "V", "W"), mixed_fields):
+        b = ref_engine.download(name)
+        out[f"rel_{name}"] = float(abs(a - b).max() / max(abs(b).max(), 1e-300))
+    out["rel_max"] = max(out["rel_U"], out["rel_V"], out["rel_W"])
+    return out
+
+
 def device_timed(e, steps: int, warmup: int, dist, clocks=None):
     """Exactly `steps` Steps timed by the step graph's event nodes (device
     time on the engine's stream), after `warmup` untimed Steps."""
@@ -288,14 +305,23 @@ def bench_mixed_512(args, dist, local, rank):
     steps = max(2, args.steps // 2)
     t = device_timed(e, steps, 1, dist)
     n = MIXED_512.n ** 3
+    md = e.MaxDivergence()
     out = {"value": n * steps * dist.world / t["dev_s"], "unit": UNIT, "steps": steps,
-           "ms_per_step": t["dev_s"] * 1e3 / steps, "max_divergence_after": e.MaxDivergence(),
+           "ms_per_step": t["dev_s"] * 1e3 / steps, "max_divergence_after": md,
            "refinement_passes_last_projection": t["passes"],
            "stages_ms_per_step": {"projections": t["solve_ms"], "sweeps": t["sweep_ms"]},
-           "workload": MIXED_512.name,
-           "error_vs_converged_fp64": "stated at 16^3 in tests/test_gpu_mixed.py: 4e-13 (one projection), "
-                                      "<=5.2e-6 relative after 5 steps (binary32 advection)"}
+           "workload": MIXED_512.name}
+    fields = velocity_host(e)
     e.Close()
+    # The same field and Steps in the FP64 form with the exact projection.
+    from aeroflux_gb300 import _lib as L
+    ref = New(MIXED_512.config(Device=local, Precision=L.AF_PRECISION_FP64))
+    ref.SeedDevice(1.0, MIXED_512.noise, 42, rank)
+    ref.applyVelocityBC()
+    ref.EnableMultigridSolver(1e-12)
+    ref.Step(1 + steps)
+    out["error_vs_fp64"] = error_vs_fp64(fields, ref, md, 1 + steps)
+    ref.Close()
     return out
 
 
@@ -331,19 +357,21 @@ def bench_batched(args, dist, local):
     passes = max(b.projection_stats(s)[0] for s in slots)
     b.close()
     value = cells * steps * dist.world / dev_s
-    # The plain FP64 form on the same mixed-size workload: a sample of the
-    # grids, each alone (GaussSeidelIters at its default).
-    sample = cfgs[:: max(1, len(cfgs) // 16)]
+    # The plain FP64 form on the same mixed-size workload: a stratified
+    # sample (every fourth grid of the generator's order, 64 grids), each
+    # alone, 10 timed Steps after one warm-up (GaussSeidelIters at its
+    # default); the aggregate is sampled cells x steps / sampled time.
+    sample = cfgs[::4]
+    k = 10
     tot_cells_steps, tot_s, divs = 0, 0.0, []
     for i, c in enumerate(sample):
-        cf = type(c)(**{k: getattr(c, k) for k in ("NX", "NY", "NZ", "H", "DT", "Viscosity", "Density")},
+        cf = type(c)(**{kk: getattr(c, kk) for kk in ("NX", "NY", "NZ", "H", "DT", "Viscosity", "Density")},
                      Device=local)
         e = New(cf)
         e.SeedDevice(1.0, 0.01, 42, i)
         e.applyVelocityBC()
         e.Step(1)
         e.Profile(True)
-        k = 3
         ms = 0.0
         for _ in range(k):
             e.Step(1)
@@ -358,6 +386,7 @@ def bench_batched(args, dist, local):
             "worst_max_divergence_after": worst, "max_refinement_passes_last_projection": passes,
             "autotune_s": tune_s, "autotuned_stages": len(tune),
             "plain_fp64_same_workload": {"value": plain, "unit": UNIT, "sample_grids": len(sample),
+                                         "sample": "every fourth grid, 10 timed Steps each",
                                          "worst_max_divergence_after": max(divs),
                                          "gauss_seidel_iters": 24},
             "speedup_vs_plain_fp64": value / plain,
@@ -373,8 +402,9 @@ def bench_served(args, local):
                        device=local)
     fp64 = run_stream_fp64(reqs, args.serve_seconds, device=local)
     return {"mixed": mixed, "plain_fp64_sequential": fp64,
-            "workload": f"Poisson arrivals at 200/s for {args.serve_seconds:g} s (of the 60 s stream), extents "
-                        "uniform over multiples of 16 in [32,192], steps uniform in [50,500], 150 GB budget",
+            "workload": f"Poisson arrivals at 200/s for {args.serve_seconds:g} s, extents uniform over multiples "
+                        "of 16 in [32,192], steps uniform in [50,500], 150 GB budget; after the arrivals end, "
+                        "requests not yet admitted are censored and the resident ones finish",
             "completed_throughput_ratio": (mixed["completed_cell_steps_per_s"] /
                                            max(fp64["completed_cell_steps_per_s"], 1e-30))}
 
@@ -452,6 +482,8 @@ def bench_ours(args):
         mv = cells * args.steps * world / tm["dev_s"]
         # Both projections of a step counted as the last one (passes and V-cycles).
         mb = mixed_bytes_per_cell_step(statistics.mean(tm["passes"]), statistics.mean(tm["vcycles"]))
+        if label == "mixed":
+            mixed_fields, mixed_md = velocity_host(em), em.MaxDivergence()
         mixed[label] = {"value": mv, "unit": UNIT, "ms_per_step": tm["dev_s"] * 1e3 / args.steps,
                         "div_tol": tol, "max_divergence_after": em.MaxDivergence(),
                         "refinement_passes_last_projection": tm["passes"],
@@ -476,6 +508,8 @@ def bench_ours(args):
                                "speedup_vs_plain": fv / value,
                                "dtype": "f64 sweeps (bit-identical to the CPU path); projection: f64 refinement "
                                         "around f32 multigrid (EnableMultigridSolver)"}
+    mixed["mixed"]["error_vs_fp64"] = error_vs_fp64(mixed_fields, ef, mixed_md, args.warmup + args.steps)
+    del mixed_fields
     ef.Close()
 
     extra = {}
@@ -528,7 +562,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--legs", default="c3,c4,c5", help="extra measurements: c3 (512^3 mixed), c4 (batched), "
                                                        "c5 (served)")
-    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

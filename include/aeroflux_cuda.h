@@ -329,6 +329,9 @@ int af_server_round(af_server* s, int64_t* completed_now, int64_t* resident, int
 int af_server_results(af_server* s, af_request_result* out, int64_t cap, int64_t* n);
 int af_server_download(af_server* s, int64_t id, int field, double* host, size_t count);
 int af_server_release(af_server* s, int64_t id);
+/* Drops every request not yet admitted (resident ones keep stepping);
+ * *cancelled gets how many. */
+int af_server_cancel_queued(af_server* s, int64_t* cancelled);
 int af_server_get_stats(af_server* s, af_server_stats* out);
 /* The batch autotuner on the requests currently resident. */
 int af_server_tune(af_server* s, int32_t reps, char* report, size_t len);
