@@ -24,6 +24,8 @@
 #include "af_batch.h"
 #include "af_cells.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -32,6 +34,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <vector>
 
 namespace af {
@@ -110,6 +113,14 @@ struct InstDev {
     FastDiv ffx, ffy, ffz;   // NX+1, NY+1, NZ+1 (the face box)
     FastDiv fnx, fny;        // NX, NY
     float* sh[3];            // binary32 shadow of the current U, V, W (the sweeps' taps)
+    int shp[3];              // row pitch of each shadow (floats): its padded x extent rounded up to 4
+    int shq[4];              // shadow conversion: prefix of the components' (row, quad) counts
+    FastDiv fsq[3];          // quads per shadow row
+    const CUtensorMap* tmap; // 12 tensor maps over the shadows: [component][role], role 0-2 the staged
+                             // tile of a sweep along axis 0-2, role 3 the axis-velocity tile
+    int sw_pre[4];           // staged sweep: prefix of the components' tile counts
+    int sw_kx0;              // first x tile of a row (tiles start at multiples of 32 in x)
+    FastDiv swx[3], swy[3];  // staged sweep, per component: tiles along x, tiles along y
     int warm;                // 1: a projection starts from the last pressure, 0: from zero
     int bc_off[10];          // velocity BC write sets: prefix of the nine (component, set) counts
     Lvl lev[kMaxLev];
@@ -124,7 +135,8 @@ enum {
     S_BIGCOARSE = S_PROLONG + kMaxLev,
     S_PAIR = S_BIGCOARSE + kMaxLev,
     S_PAIRN = S_PAIR + kMaxLev,
-    S_COUNT = S_PAIRN + kMaxLev
+    S_SWEEPT = S_PAIRN + kMaxLev,
+    S_COUNT = S_SWEEPT + 1
 };
 
 struct Shape {
@@ -267,28 +279,31 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
 }
 
 // binary32 shadow of the current U, V, W (every element, ghosts included),
-// converted once per sweep instead of once per tap.  A thread converts four
-// consecutive elements of one field (two 16-byte loads, one 16-byte store;
-// fields start on 128-byte boundaries); the iteration space counts quads.
-__host__ __device__ inline long long quads(long long n) { return (n + 3) / 4; }
-
+// converted once per sweep instead of once per tap.  A shadow row holds the
+// field row's nx values and is padded to a multiple of four floats (the row
+// pitch shp), so rows start on 16-byte boundaries and a TMA tensor map can
+// describe the shadow.  A thread converts four consecutive elements of one
+// row and stores them with one 16-byte store (padding: zeros).
 __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
-    const long long qu = quads(I.g.u.count), qv = quads(I.g.v.count), n = qu + qv + quads(I.g.w.count);
+    const long long n = I.shq[3];
     FOR_ELEMS(tab)
     if (el >= n) break;
-    const int f = el < qu ? 0 : (el < qu + qv ? 1 : 2);
-    const long long q = el - (f == 0 ? 0 : (f == 1 ? qu : qu + qv));
-    const long long count = f == 0 ? I.g.u.count : (f == 1 ? I.g.v.count : I.g.w.count);
-    const double* src = cur(I, 1 + f, parity) + 4 * q;
-    float* dst = I.sh[f] + 4 * q;
-    if (4 * q + 4 <= count) {
-        const double2 a = reinterpret_cast<const double2*>(src)[0], b = reinterpret_cast<const double2*>(src)[1];
-        reinterpret_cast<float4*>(dst)[0] = make_float4(f64_to_f32(a.x), f64_to_f32(a.y), f64_to_f32(b.x), f64_to_f32(b.y));
-    } else {
-        for (long long k = 0; 4 * q + k < count; ++k) dst[k] = f64_to_f32(src[k]);
-    }
+    const int e = (int)el;
+    const int f = e < I.shq[1] ? 0 : (e < I.shq[2] ? 1 : 2);
+    const unsigned r = (unsigned)(e - I.shq[f]);
+    const unsigned row = I.fsq[f].div(r), q = r - row * I.fsq[f].d;
+    const Dims& d = f == 0 ? I.g.u : (f == 1 ? I.g.v : I.g.w);
+    const double* src = cur(I, 1 + f, parity) + (long long)row * d.nx + 4 * q;
+    float* dst = I.sh[f] + (long long)row * I.shp[f] + 4 * q;
+    const int left = d.nx - 4 * (int)q;
+    float4 o;
+    o.x = f64_to_f32(src[0]);
+    o.y = left > 1 ? f64_to_f32(src[1]) : 0.0f;
+    o.z = left > 2 ? f64_to_f32(src[2]) : 0.0f;
+    o.w = left > 3 ? f64_to_f32(src[3]) : 0.0f;
+    *reinterpret_cast<float4*>(dst) = o;
     END_ELEMS
     END_TILES
 }
@@ -306,15 +321,15 @@ __device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* 
     const Geom& g = I.g;
     const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
     const Dims& a = AX == 0 ? g.u : (AX == 1 ? g.v : g.w);
-    const long long rb = (long long)y * d.sy + (long long)z * d.sz;
-    const float* __restrict__ src = I.sh[C] + rb;
-    dd += rb;
-    const int s = AX == 0 ? 1 : (AX == 1 ? (int)d.sy : (int)d.sz);
+    const long long py = I.shp[C], pz = py * d.ny;  // shadow strides
+    const float* __restrict__ src = I.sh[C] + y * py + z * pz;
+    dd += (long long)y * d.sy + (long long)z * d.sz;
+    const long long s = AX == 0 ? 1 : (AX == 1 ? py : pz);
     const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
     // Face velocity taps (summed by mx_face_vel4): offsets from (x, y, z) in the axis
-    // component, in the order they are summed.
-    const float* __restrict__ va = I.sh[AX] + (long long)y * a.sy + (long long)z * a.sz;
-    const int ay = (int)a.sy, az = (int)a.sz;
+    // component's shadow, in the order they are summed.
+    const int ay = I.shp[AX], az = I.shp[AX] * a.ny;
+    const float* __restrict__ va = I.sh[AX] + (long long)y * ay + (long long)z * az;
     int o0 = 0, o1 = 0, o2 = 0, o3 = 0;
     if (C == 0 && AX == 1) { o0 = -1; o1 = 0; o2 = ay - 1; o3 = ay; }
     if (C == 0 && AX == 2) { o0 = -1; o1 = 0; o2 = az - 1; o3 = az; }
@@ -381,6 +396,190 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
     else sweep_row<AX, 2>(I, st + s, cur(I, 7, parity), y, z, x0, x1, phase);
     END_ELEMS
     END_TILES
+}
+
+// --- staged tile sweep ---------------------------------------------------
+// The same sweep with its gathers served from shared memory.  A block owns a
+// tile of kSwTX x kSwTY x kSwTZ faces of one component (x tiles start at
+// multiples of 32, so every staged box starts on a 16-byte boundary).  One
+// thread stages, with TMA tensor loads over the binary32 shadows, the tile
+// of the face's own component with a halo along the sweep axis (4 cells
+// along x, kSwHA along y or z: the diffusion taps and every backtrace with
+// |dt*vel/h| < kSwHA) and, when the component is not the sweep axis's, the
+// tile of the axis component whose four faces give the face velocity (a
+// one-cell halo).  Backtraces that leave the staged halo read the shadow in
+// global memory instead.  Every face's arithmetic is the row kernel's
+// (mx_face_vel4, mx_backtrace, mx_face_value): the same bits.
+constexpr int kSwTX = 32, kSwTY = 8, kSwTZ = 4, kSwHA = 2, kSwThreads = kSwTX * kSwTY;
+__host__ __device__ constexpr int sw_bx(int role) { return role == 0 || role == 3 ? kSwTX + 8 : kSwTX; }
+__host__ __device__ constexpr int sw_by(int role) {
+    return role == 1 ? kSwTY + 2 * kSwHA : (role == 3 ? kSwTY + 2 : kSwTY);
+}
+__host__ __device__ constexpr int sw_bz(int role) {
+    return role == 2 ? kSwTZ + 2 * kSwHA : (role == 3 ? kSwTZ + 2 : kSwTZ);
+}
+constexpr int kSwOwnMax = 2048;  // floats of the largest own-component box (sweep along z)
+constexpr int kSwAxCount = (kSwTX + 8) * (kSwTY + 2) * (kSwTZ + 2);
+static_assert(sw_bx(0) * sw_by(0) * sw_bz(0) <= kSwOwnMax && sw_bx(1) * sw_by(1) * sw_bz(1) <= kSwOwnMax &&
+              sw_bx(2) * sw_by(2) * sw_bz(2) <= kSwOwnMax, "own box exceeds its buffer");
+static_assert(sw_bx(3) * sw_by(3) * sw_bz(3) == kSwAxCount, "axis box size");
+// A wait on a TMA transfer gives up after this many polls (each poll itself
+// blocks for a bounded, hardware-defined time); the kernel then records the
+// failure in the batch's diagnostic word and returns.
+constexpr unsigned kSwSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Polls the barrier's phase `parity` at most kSwSpinLimit times.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+    for (unsigned it = 0; it < kSwSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_addr(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Faces of one tile of component C (the loads have landed in own / axv).
+template <int AX, int C>
+__device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, const float* own, const float* axv,
+                                                 double* __restrict__ dd, int x0, int y0, int z0, int phase) {
+    const Geom& g = I.g;
+    const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
+    constexpr int BX = sw_bx(AX), BY = sw_by(AX), BZ = sw_bz(AX);
+    constexpr int SO = AX == 0 ? 1 : (AX == 1 ? BX : BX * BY);  // own-box stride along the sweep axis
+    constexpr int AXX = kSwTX + 8, AXY = kSwTY + 2;
+    // Axis-box strides along the component's axis and the sweep axis.
+    constexpr int EC = C == 0 ? 1 : (C == 1 ? AXX : AXX * AXY);
+    constexpr int EA = AX == 0 ? 1 : (AX == 1 ? AXX : AXX * AXY);
+    const int ox = x0 - (AX == 0 ? 4 : 0), oy = y0 - (AX == 1 ? kSwHA : 0), oz = z0 - (AX == 2 ? kSwHA : 0);
+    const int oa = AX == 0 ? ox : (AX == 1 ? oy : oz);  // own box's first coordinate along the axis
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    const int x = x0 + lx, y = y0 + ly;
+    const int G = g.G;
+    if (x < G || x >= G + g.NX + (C == 0) || y >= G + g.NY + (C == 1)) return;
+    const int zend = min(z0 + kSwTZ, G + g.NZ + (C == 2));
+    const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+    const long long py = I.shp[C], pz = py * d.ny;
+    const long long gs = AX == 0 ? 1 : (AX == 1 ? py : pz);
+    const float dt_invh = I.dt_invh, lam = I.lam;
+    for (int z = z0; z < zend; ++z) {
+        const int io = ((z - oz) * BY + (y - oy)) * BX + (x - ox);
+        float vel;
+        if (C == AX) {
+            vel = own[io];
+        } else {
+            const int ia = ((z - z0 + 1) * AXY + (y - y0 + 1)) * AXX + (x - x0 + 4);
+            // The row kernel's tap order: before the sweep axis's own
+            // component, (-e_C, 0, e_AX - e_C, e_AX); after it,
+            // (-e_C, e_AX - e_C, 0, e_AX).
+            if (AX > C) vel = mx_face_vel4(axv[ia - EC], axv[ia], axv[ia + EA - EC], axv[ia + EA]);
+            else vel = mx_face_vel4(axv[ia - EC], axv[ia + EA - EC], axv[ia], axv[ia + EA]);
+        }
+        const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+        int i0;
+        float t;
+        if (!mx_backtrace(vel, ca, na, dt_invh, &i0, &t)) {
+            atomicMin(&st->fault_gate, st->step * 8u + (unsigned)phase);
+            atomicMin(&st->fault_key, fault_key(C, x, y, z));
+            continue;
+        }
+        float d0, d1;
+        const int rel = i0 - ca;
+        if (i0 >= oa && i0 + 1 < oa + (AX == 0 ? BX : (AX == 1 ? BY : BZ))) {
+            d0 = own[io + rel * SO];
+            d1 = own[io + (rel + 1) * SO];
+        } else {
+            const float* gp = I.sh[C] + x + y * py + z * pz + rel * gs;
+            d0 = gp[0];
+            d1 = gp[gs];
+        }
+        const float res = mx_face_value(t, d0, d1, own[io - SO], own[io], own[io + SO], lam);
+        dd[x + (long long)y * d.sy + (long long)z * d.sz] = (double)res;  // widening is exact
+    }
+}
+
+template <int AX, int C>
+__device__ __forceinline__ bool sweep_tile(const InstDev& I, Status* st, float* own, float* axv,
+                                           unsigned long long* bar, unsigned* ph, double* dd, int x0, int y0, int z0,
+                                           int phase) {
+    if (threadIdx.x == 0) {
+        // The previous tile's reads of the buffers (generic proxy) precede
+        // these TMA writes (async proxy).
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        constexpr unsigned own_bytes = sw_bx(AX) * sw_by(AX) * sw_bz(AX) * 4u;
+        mbar_expect_tx(bar, own_bytes + (C != AX ? kSwAxCount * 4u : 0u));
+        tma_load_3d(own, I.tmap + C * 4 + AX, x0 - (AX == 0 ? 4 : 0), y0 - (AX == 1 ? kSwHA : 0),
+                    z0 - (AX == 2 ? kSwHA : 0), bar);
+        if (C != AX) tma_load_3d(axv, I.tmap + AX * 4 + 3, x0 - 4, y0 - 1, z0 - 1, bar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *ph) ? 1 : 0) != 0;
+    *ph ^= 1u;
+    if (!ok) return false;
+    sweep_tile_faces<AX, C>(I, st, own, axv, dd, x0, y0, z0, phase);
+    return true;
+}
+
+template <int AX>
+__global__ void __launch_bounds__(kSwThreads, 4)
+    kb_sweep_tma(const InstDev* inst, Status* st, Tab tab, int parity, int phase, unsigned* diag) {
+    __shared__ __align__(128) float own[kSwOwnMax];
+    __shared__ __align__(128) float axv[kSwAxCount];
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned ph = 0;
+    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
+        const int s = find_slot(tab.prefix, tab.n, item);
+        const InstDev& I = inst[s];
+        if (gated(&st[s], phase)) continue;
+        const int local = item - tab.prefix[s];
+        const int c = local >= I.sw_pre[2] ? 2 : (local >= I.sw_pre[1] ? 1 : 0);
+        const unsigned r = (unsigned)(local - I.sw_pre[c]);
+        const unsigned q1 = I.swx[c].div(r), q2 = I.swy[c].div(q1);
+        const int x0 = (I.sw_kx0 + (int)(r - q1 * I.swx[c].d)) * kSwTX;
+        const int y0 = I.g.G + (int)(q1 - q2 * I.swy[c].d) * kSwTY;
+        const int z0 = I.g.G + (int)q2 * kSwTZ;
+        double* dd = cur(I, 5 + c, parity);
+        bool ok;
+        if (c == 0) ok = sweep_tile<AX, 0>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
+        else if (c == 1) ok = sweep_tile<AX, 1>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
+        else ok = sweep_tile<AX, 2>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
+        if (!ok) {
+            // The transfer did not land in time: record it, give the copies in
+            // flight a second bounded wait, and stop.
+            if (threadIdx.x == 0) {
+                atomicOr(diag, 1u);
+                mbar_wait_bounded(&bar, ph ^ 1u);
+            }
+            __syncthreads();
+            return;
+        }
+        __syncthreads();  // every thread is done with the buffers before the next tile's loads
+    }
 }
 
 __global__ void kb_tick(const InstDev* inst, Status* st, int n) {
@@ -1168,6 +1367,11 @@ struct Batch {
     double pass_floor = 0.0;  // max|r| reduction one pass can reach (0: not used to cut V-cycles)
     int fixed_passes = 0;
     cudaError_t capture_err = cudaSuccess;
+    bool tma_sweep = true;             // staged tile sweep (false: the row kernel)
+    CUtensorMap* d_tmaps = nullptr;    // 12 per slot, see InstDev::tmap
+    std::vector<CUtensorMap> h_tmaps;
+    bool tmaps_dirty = true;
+    unsigned* d_diag = nullptr;        // nonzero: a kernel gave up waiting on a transfer
 };
 
 namespace {
@@ -1230,7 +1434,8 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     if (st == S_BC) n = bc_count(I.g);
     else if (st == S_SWEEP) n = sweep_box(I.g);
     else if (st == S_GRAD) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
-    else if (st == S_SHADOW) n = quads(I.g.u.count) + quads(I.g.v.count) + quads(I.g.w.count);
+    else if (st == S_SHADOW) n = I.shq[3];
+    else if (st == S_SWEEPT) return I.sw_pre[3];
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
     else if (st == S_CORR) n = 32ll * I.g.NY * I.g.NZ;
@@ -1286,6 +1491,12 @@ cudaError_t upload_tables(Batch* b) {
     if ((rc = cudaMemcpyAsync(b->d_inst, inst.data(), inst.size() * sizeof(InstDev), cudaMemcpyHostToDevice,
                               b->stream)) != cudaSuccess)
         return rc;
+    if (b->tmaps_dirty) {
+        if ((rc = cudaMemcpyAsync(b->d_tmaps, b->h_tmaps.data(), b->h_tmaps.size() * sizeof(CUtensorMap),
+                                  cudaMemcpyHostToDevice, b->stream)) != cudaSuccess)
+            return rc;
+        b->tmaps_dirty = false;
+    }
     b->tables_dirty = false;
     return cudaStreamSynchronize(b->stream);
 }
@@ -1318,6 +1529,13 @@ void enq_bc(Batch* b, int parity, int gate, cudaStream_t s) { LAUNCH(b, S_BC, kb
 
 void enq_sweep(Batch* b, int axis, int parity, int phase, cudaStream_t s) {
     LAUNCH(b, S_SHADOW, kb_shadow, b->d_inst, tab(b, S_SHADOW), parity);
+    if (b->tma_sweep) {
+        const Tab t = tab(b, S_SWEEPT);
+        if (axis == 0) LAUNCH(b, S_SWEEPT, kb_sweep_tma<0>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        else if (axis == 1) LAUNCH(b, S_SWEEPT, kb_sweep_tma<1>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        else LAUNCH(b, S_SWEEPT, kb_sweep_tma<2>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        return;
+    }
     const Tab t = tab(b, S_SWEEP);
     if (axis == 0) LAUNCH(b, S_SWEEP, kb_sweep<0>, b->d_inst, b->d_st, t, parity, phase);
     else if (axis == 1) LAUNCH(b, S_SWEEP, kb_sweep<1>, b->d_inst, b->d_st, t, parity, phase);
@@ -1522,6 +1740,50 @@ cudaError_t reset_status(Batch* b) {
 
 std::string fault_message_for(const Geom& g, unsigned gate, unsigned long long key);
 
+namespace {
+
+// cuTensorMapEncodeTiled from the driver, resolved once through the runtime
+// (the library links no driver stub); NULL when the driver lacks it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The 12 tensor maps of a slot over its three binary32 shadows: per
+// component, the staged boxes of a sweep along x, y and z and the
+// axis-velocity box.  Out-of-range box elements load as zeros (never read).
+bool encode_slot_maps(const InstDev& I, CUtensorMap* maps) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    for (int k = 0; k < 3; ++k) {
+        const Dims& d = k == 0 ? I.g.u : (k == 1 ? I.g.v : I.g.w);
+        const cuuint64_t dims[3] = {(cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
+        const cuuint64_t strides[2] = {(cuuint64_t)I.shp[k] * 4u, (cuuint64_t)I.shp[k] * d.ny * 4u};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        for (int role = 0; role < 4; ++role) {
+            const cuuint32_t box[3] = {(cuuint32_t)sw_bx(role), (cuuint32_t)sw_by(role), (cuuint32_t)sw_bz(role)};
+            if (enc(&maps[k * 4 + role], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, I.sh[k], dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return false;
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // Host API
 // ---------------------------------------------------------------------------
@@ -1543,6 +1805,10 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     if (const char* cs = getenv("AEROFLUX_COLD_START")) b->cold = atoi(cs) != 0;
     if (const char* vc = getenv("AEROFLUX_MG_VCYCLES")) b->vcycles = std::min(8, std::max(1, atoi(vc)));
     if (const char* pf = getenv("AEROFLUX_MG_PASS_FLOOR")) b->pass_floor = atoi(pf) < 0 ? ldexp(1.0, atoi(pf)) : 0.0;
+    // The row sweep (gathers through L1) instead of the staged tile sweep: the same bits.
+    if (const char* sr = getenv("AEROFLUX_SWEEP_ROWS")) b->tma_sweep = atoi(sr) == 0;
+    if (b->tma_sweep && !tensor_map_encoder()) b->tma_sweep = false;
+    b->shape[S_SWEEPT] = Shape{kSwThreads, 1, 4};
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) {
@@ -1555,12 +1821,16 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
         (rc = cudaMalloc(&b->d_inst, sizeof(InstDev) * capacity)) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_st, sizeof(Status) * capacity)) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_ctl, sizeof(Ctl) * (capacity + 1))) != cudaSuccess ||
-        (rc = cudaMalloc(&b->d_tab, sizeof(int) * (size_t)S_COUNT * (capacity + 1))) != cudaSuccess) {
+        (rc = cudaMalloc(&b->d_tab, sizeof(int) * (size_t)S_COUNT * (capacity + 1))) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_tmaps, sizeof(CUtensorMap) * 12 * (size_t)capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_diag, sizeof(unsigned))) != cudaSuccess) {
         *err = std::string("aeroflux: batch tables: ") + cudaGetErrorString(rc);
         batch_destroy(b);
         return nullptr;
     }
     cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl) * (capacity + 1), b->stream);
+    cudaMemsetAsync(b->d_diag, 0, sizeof(unsigned), b->stream);
+    b->h_tmaps.assign(12 * (size_t)capacity, CUtensorMap{});
     if (pool_bytes) {
         if (!b->pool.init(pool_bytes)) {
             *err = "aeroflux: batch device pool of " + std::to_string(pool_bytes) + " bytes: out of memory";
@@ -1590,6 +1860,8 @@ void batch_destroy(Batch* b) {
     cudaFree(b->d_st);
     cudaFree(b->d_ctl);
     cudaFree(b->d_tab);
+    cudaFree(b->d_tmaps);
+    cudaFree(b->d_diag);
     if (b->body) cudaStreamDestroy(b->body);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1706,7 +1978,8 @@ size_t batch_slot_bytes(const af_config& c) {
     const size_t arena = ((size_t)off + 255) & ~(size_t)255;
     const size_t bb = ((size_t)(cx * cy * cz) * 8 + 255) & ~(size_t)255;
     auto al = [](int64_t n) { return ((size_t)n * 4 + 255) & ~(size_t)255; };
-    const size_t shb = al((cx + 1) * cy * cz) + al(cx * (cy + 1) * cz) + al(cx * cy * (cz + 1));
+    auto pitch = [](int64_t nx) { return (nx + 3) / 4 * 4; };
+    const size_t shb = al(pitch(cx + 1) * cy * cz) + al(pitch(cx) * (cy + 1) * cz) + al(pitch(cx) * cy * (cz + 1));
     Lvl lev[kMaxLev];
     int cs = 0, tf = 0;
     const int nl = plan_levels((int)c.nx, (int)c.ny, (int)c.nz, lev, &cs);
@@ -1791,7 +2064,35 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     const size_t arena_bytes = ((size_t)off + 255) & ~(size_t)255;
     const size_t b_bytes = ((size_t)S.desc[0].count * 8 + 255) & ~(size_t)255;
     size_t sh_bytes[3];
-    for (int k = 0; k < 3; ++k) sh_bytes[k] = ((size_t)S.desc[1 + k].count * 4 + 255) & ~(size_t)255;
+    for (int k = 0; k < 3; ++k) {
+        const af_field_desc& d = S.desc[1 + k];
+        I.shp[k] = (int)((d.nx + 3) / 4 * 4);
+        sh_bytes[k] = ((size_t)I.shp[k] * d.ny * d.nz * 4 + 255) & ~(size_t)255;
+    }
+    {
+        // Shadow conversion: (row, quad) items per component.
+        int acc = 0;
+        for (int k = 0; k < 3; ++k) {
+            const af_field_desc& d = S.desc[1 + k];
+            I.shq[k] = acc;
+            I.fsq[k] = FastDiv((unsigned)(I.shp[k] / 4));
+            acc += (int)(d.ny * d.nz * (I.shp[k] / 4));
+        }
+        I.shq[3] = acc;
+        // Staged sweep tiles per component: x tiles from x = 32 * (G / 32)
+        // to the component's last face, y and z tiles from G.
+        I.sw_kx0 = I.g.G / kSwTX;
+        I.sw_pre[0] = 0;
+        for (int k = 0; k < 3; ++k) {
+            const int xend = I.g.G + I.g.NX + (k == 0);
+            const int ntx = (xend - 1) / kSwTX - I.sw_kx0 + 1;
+            const int nty = (I.g.NY + (k == 1) + kSwTY - 1) / kSwTY;
+            const int ntz = (I.g.NZ + (k == 2) + kSwTZ - 1) / kSwTZ;
+            I.swx[k] = FastDiv((unsigned)ntx);
+            I.swy[k] = FastDiv((unsigned)nty);
+            I.sw_pre[k + 1] = I.sw_pre[k] + ntx * nty * ntz;
+        }
+    }
     size_t mg = 0;
     for (int l = 0; l < I.nlev; ++l) mg += (pair_level(l) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
     mg = (mg + 255) & ~(size_t)255;
@@ -1823,6 +2124,16 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
     for (int k = 0; k < 3; ++k) {
         I.sh[k] = (float*)p;
         p += sh_bytes[k];
+    }
+    I.tmap = b->d_tmaps + 12 * (size_t)s;
+    b->tmaps_dirty = true;
+    if (b->tma_sweep && !encode_slot_maps(I, &b->h_tmaps[12 * (size_t)s])) {
+        // No tensor maps for this slot: the whole batch sweeps with the row kernel.
+        b->tma_sweep = false;
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
     }
     float* fp = (float*)p;
     for (int l = 0; l < I.nlev; ++l) {
@@ -2045,6 +2356,17 @@ int batch_collect_faults(Batch* b, std::string* msg, int* first_slot) {
     return n;
 }
 
+bool batch_device_error(Batch* b, std::string* msg) {
+    unsigned v = 0;
+    cudaStreamSynchronize(b->stream);
+    cudaMemcpy(&v, b->d_diag, sizeof v, cudaMemcpyDeviceToHost);
+    if (!v) return false;
+    cudaMemset(b->d_diag, 0, sizeof v);
+    *msg = "aeroflux: cuda: a staged-sweep kernel gave up waiting for its tile transfer; the step's results are "
+           "invalid";
+    return true;
+}
+
 bool batch_slot_faulted(const Batch* b, int s, std::string* msg) {
     Status st;
     cudaMemcpy(&st, b->d_st + s, sizeof st, cudaMemcpyDeviceToHost);
@@ -2130,7 +2452,8 @@ std::string batch_tune(Batch* b, int reps) {
         else if (st >= S_PROLONG && st < S_BIGCOARSE)
             kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG, 0);
     };
-    std::vector<int> stages = {S_BC, S_SHADOW, S_SWEEP, S_DIV, S_INT, S_PBC, S_GRAD};
+    std::vector<int> stages = {S_BC, S_SHADOW, S_DIV, S_INT, S_PBC, S_GRAD};
+    if (!b->tma_sweep) stages.push_back(S_SWEEP);  // the staged sweep keeps its fixed tile shape
     for (int l = 0; l + 1 < L; ++l) {
         stages.push_back(S_SMOOTH + l);
         stages.push_back(S_RESTRICT + l);

@@ -68,6 +68,9 @@ cudaError_t batch_seed(Batch* b, int slot, double amp, double noise, uint64_t se
 // slots that faulted in it; `msg` gets the first faulting slot's message.
 int batch_collect_faults(Batch* b, std::string* msg, int* first_slot);
 bool batch_slot_faulted(const Batch* b, int slot, std::string* msg);
+// Whether a kernel of the enqueued work gave up a bounded wait (the work's
+// results are then invalid); clears the record and sets *msg.
+bool batch_device_error(Batch* b, std::string* msg);
 // Refinement passes, estimated max|div| and multigrid V-cycles of the slot's
 // last projection.
 void batch_slot_projection(Batch* b, int slot, int64_t* passes, double* max_div, int64_t* vcycles = nullptr);

@@ -374,16 +374,14 @@ __device__ __forceinline__ float mx_face_vel4(float t0, float t1, float t2, floa
     return __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3));
 }
 
-// New value of the face whose binary32 value sits at f[0] (its neighbours
-// along the sweep axis at f[-s] and f[s]; ca is its coordinate on that axis,
-// na the field's padded extent there): the semi-Lagrangian backtrace by
-// velocity vel, relative to the face so binary32 keeps the fraction accurate
-// at any grid size (departure = ca + off, off = -dt*vel/h), clamped into the
-// padded field as stencil.go:174-188 clamps, linear interpolation
-// d0 + t*(d1 - d0), plus lam times the second difference.  Returns false on
-// a NaN backtrace (a contained fault; the face is then not written).
-__device__ __forceinline__ bool mx_face_update(const float* __restrict__ f, int s, float vel, int ca, int na,
-                                               float dt_invh, float lam, float* out) {
+// Semi-Lagrangian backtrace of a face at coordinate ca (na: the field's
+// padded extent along the sweep axis) by velocity vel, relative to the face
+// so binary32 keeps the fraction accurate at any grid size (departure =
+// ca + off, off = -dt*vel/h), clamped into the padded field as
+// stencil.go:174-188 clamps: the interpolation taps are i0 and i0 + 1 with
+// weight t on the second.  Returns false on a NaN backtrace (a contained
+// fault; the face is then not written).
+__device__ __forceinline__ bool mx_backtrace(float vel, int ca, int na, float dt_invh, int* i0_out, float* t_out) {
     const float off = -__fmul_rn(vel, dt_invh);
     if (isnan(off)) return false;
     const float fl = floorf(off);
@@ -404,11 +402,29 @@ __device__ __forceinline__ bool mx_face_update(const float* __restrict__ f, int 
             t = 1.0f;
         }
     }
-    const float* p0 = f + (long long)(i0 - ca) * s;
-    const float d0 = p0[0], d1 = p0[s];
+    *i0_out = i0;
+    *t_out = t;
+    return true;
+}
+
+// Linear interpolation d0 + t*(d1 - d0) plus lam times the second
+// difference (fm - 2 f0) + fp of the face's own values along the axis.
+__device__ __forceinline__ float mx_face_value(float t, float d0, float d1, float fm, float f0, float fp, float lam) {
     const float adv = __fmaf_rn(t, __fsub_rn(d1, d0), d0);
-    if (lam != 0.0f) *out = __fmaf_rn(lam, __fadd_rn(__fsub_rn(f[-s], __fmul_rn(2.0f, f[0])), f[s]), adv);
-    else *out = __fadd_rn(adv, 0.0f);
+    if (lam != 0.0f) return __fmaf_rn(lam, __fadd_rn(__fsub_rn(fm, __fmul_rn(2.0f, f0)), fp), adv);
+    return __fadd_rn(adv, 0.0f);
+}
+
+// New value of the face whose binary32 value sits at f[0] (its neighbours
+// along the sweep axis at f[-s] and f[s]): mx_backtrace, then mx_face_value
+// with the taps read through f.
+__device__ __forceinline__ bool mx_face_update(const float* __restrict__ f, long long s, float vel, int ca, int na,
+                                               float dt_invh, float lam, float* out) {
+    int i0;
+    float t;
+    if (!mx_backtrace(vel, ca, na, dt_invh, &i0, &t)) return false;
+    const float* p0 = f + (long long)(i0 - ca) * s;
+    *out = mx_face_value(t, p0[0], p0[s], f[-s], f[0], f[s], lam);
     return true;
 }
 

@@ -464,6 +464,10 @@ int batch_check(af_engine* e, cudaError_t rc, const std::string& what) {
     if ((rc = cudaStreamSynchronize(af::batch_stream(e->batch))) != cudaSuccess) return cuda_fail(e, rc, "batch");
     std::string msg;
     int first = -1;
+    if (af::batch_device_error(e->batch, &msg)) {
+        e->err = msg;
+        return AF_ERR_CUDA;
+    }
     if (af::batch_collect_faults(e->batch, &msg, &first)) {
         e->err = msg;
         return AF_ERR_FAULT;
@@ -1162,6 +1166,7 @@ int af_batch_step(af_batch* h, int64_t nsteps) {
     cudaError_t rc = af::batch_step(h->b, nsteps, &m);
     if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, m);
     if (int r = batch_wait(h)) return r;
+    if (af::batch_device_error(h->b, &m)) return batch_fail(h, AF_ERR_CUDA, m);
     int first = -1;
     af::batch_collect_faults(h->b, &m, &first);
     return AF_OK;

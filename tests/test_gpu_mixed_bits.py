@@ -31,7 +31,9 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(16, 16, 16), (32, 32, 32), (96, 40, 36), (33, 17, 20), (65, 24, 16), (97, 34, 18), (24, 20, 18),
           (48, 32, 96), (1, 1, 1), (40, 1, 1), (3, 2, 5), (35, 33, 37)]
 ENV_KEYS = ("AEROFLUX_FIXED_REFINEMENT_PASSES", "AEROFLUX_MG_VCYCLES", "AEROFLUX_COLD_START",
-            "AEROFLUX_MG_PER_LEVEL", "AEROFLUX_MG_PAIRS", "AEROFLUX_MG_PASS_FLOOR")
+            "AEROFLUX_MG_PER_LEVEL", "AEROFLUX_MG_PAIRS", "AEROFLUX_MG_PASS_FLOOR", "AEROFLUX_SWEEP_ROWS")
+# The staged tile sweep (default) and the row sweep compute the same bits.
+SWEEPS = {"staged": {}, "rows": {"AEROFLUX_SWEEP_ROWS": 1}}
 
 
 @contextlib.contextmanager
@@ -93,22 +95,25 @@ def assert_same(gpu_fields, orc, names=FIELDS, what=""):
                                  f"gpu={g[bad[0]]!r} oracle={ref[bad[0]]!r}")
 
 
+@pytest.mark.parametrize("kind", sorted(SWEEPS))
 @pytest.mark.parametrize("n", SHAPES)
 @pytest.mark.parametrize("axis", [0, 1, 2])
-def test_binary32_sweep_bit_exact(n, axis):
-    e, o = make_mixed_pair(n)
+def test_binary32_sweep_bit_exact(n, axis, kind):
+    e, o = make_mixed_pair(n, env_kw=SWEEPS[kind])
     e.sweep(axis, 0.002)
     o.sweep(axis, 0.002)
     assert_same(e.download, o, ("U", "V", "W", "Tmp0", "Tmp1", "Tmp2"), f"{n} axis {axis}")
     e.Close()
 
 
+@pytest.mark.parametrize("kind", sorted(SWEEPS))
 @pytest.mark.parametrize("axis", [0, 1, 2])
-def test_binary32_sweep_random_ghosts_and_clamped_backtraces(axis):
+def test_binary32_sweep_random_ghosts_and_clamped_backtraces(axis, kind):
     # Random data in every element (ghosts and never-written planes
-    # included, no BC) at amplitude 25: backtraces leave the field and clamp.
+    # included, no BC) at amplitude 25: backtraces leave the field and clamp,
+    # most of them beyond the staged halo (the global fallback).
     n = (20, 14, 11)
-    e, o = make_mixed_pair(n, apply_bc=False)
+    e, o = make_mixed_pair(n, apply_bc=False, env_kw=SWEEPS[kind])
     rng = np.random.default_rng(7 + axis)
     for i, name in enumerate(("U", "V", "W"), start=1):
         a = rng.uniform(-25, 25, o.data(i).size)
