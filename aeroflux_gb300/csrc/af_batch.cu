@@ -70,7 +70,8 @@ struct Lvl {
     float* r;
     FastDiv fnx, fny, fhx;  // nx, ny, (nx+1)/2
     float* e2;              // second buffer of the fused red-black pair (levels below the tail)
-    FastDiv ftx, fty;       // fused-pair wide tiles along x and tiles along y
+    FastDiv ftx;            // fused-pair wide tiles along x
+    FastDiv fty[3];         // fused-pair tiles along y, per tile variant (kPairVarTY)
     int nxw;                // 64 x the wide pair tiles along x; a narrow tile column covers nxw .. nx-1
 };
 
@@ -119,7 +120,6 @@ struct InstDev {
     const CUtensorMap* tmap; // 12 tensor maps over the shadows: [component][role], role 0-2 the staged
                              // tile of a sweep along axis 0-2, role 3 the axis-velocity tile
     int sw_pre[4];           // staged sweep: prefix of the components' tile counts
-    int sw_kx0;              // first x tile of a row (tiles start at multiples of 32 in x)
     FastDiv swx[3], swy[3];  // staged sweep, per component: tiles along x, tiles along y
     int warm;                // 1: a projection starts from the last pressure, 0: from zero
     int bc_off[10];          // velocity BC write sets: prefix of the nine (component, set) counts
@@ -143,6 +143,7 @@ struct Shape {
     int tpb = 256;   // threads per block
     int ept = 1;     // elements per thread
     int bpsm = 8;    // persistent blocks per SM
+    int var = 0;     // fused-pair stages: the tile variant (kPairVarTY, kPairVarTZ)
 };
 
 // A stage's device work list: prefix[0..n] of tiles per slot.
@@ -255,7 +256,9 @@ __global__ void kb_pbc(const InstDev* inst, Status* st, Tab tab, int gate) {
 }
 
 // subtractGradient over every face, a warp per (component, y, z) face row.
-__global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, int gate) {
+// scratch = 1 (the autotuner's timing runs) stores the new values into the
+// Tmp fields instead, so timing leaves the slots' velocities untouched.
+__global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, int gate, int scratch) {
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (gated(&st[s], gate)) continue;
@@ -273,7 +276,9 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
     const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
     if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
     const int x1 = g.G + g.NX + (c == 0);
-    for (int x = g.G + lane; x < x1; x += 32) grad_face(g, I.slot[0], u, v, w, I.grad_scale, c, x, y, z);
+    const double* f = c == 0 ? u : (c == 1 ? v : w);
+    double* out = scratch ? cur(I, 5 + c, parity) : (c == 0 ? u : (c == 1 ? v : w));
+    for (int x = g.G + lane; x < x1; x += 32) grad_face_to(g, I.slot[0], f, out, I.grad_scale, c, x, y, z);
     END_ELEMS
     END_TILES
 }
@@ -400,25 +405,35 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
 
 // --- staged tile sweep ---------------------------------------------------
 // The same sweep with its gathers served from shared memory.  A block owns a
-// tile of kSwTX x kSwTY x kSwTZ faces of one component (x tiles start at
-// multiples of 32, so every staged box starts on a 16-byte boundary).  One
-// thread stages, with TMA tensor loads over the binary32 shadows, the tile
-// of the face's own component with a halo along the sweep axis (4 cells
-// along x, kSwHA along y or z: the diffusion taps and every backtrace with
-// |dt*vel/h| < kSwHA) and, when the component is not the sweep axis's, the
-// tile of the axis component whose four faces give the face velocity (a
-// one-cell halo).  Backtraces that leave the staged halo read the shadow in
-// global memory instead.  Every face's arithmetic is the row kernel's
-// (mx_face_vel4, mx_backtrace, mx_face_value): the same bits.
+// tile of kSwTX x kSwTY x kSwTZ faces of one component, x tiles starting at
+// the first interior face (G + 32k; a U row's extra last face joins its last
+// tile).  One thread stages, with TMA tensor loads over the binary32
+// shadows, the tile of the face's own component with a halo along the sweep
+// axis (at least 4 cells along x, kSwHA along y or z: the diffusion taps and
+// every backtrace with |dt*vel/h| < kSwHA) and, when the component is not
+// the sweep axis's, the tile of the axis component whose four faces give the
+// face velocity (a one-cell halo).  A TMA box must start on a 16-byte
+// boundary, so each box starts at the x below its tile's halo rounded down
+// to a multiple of four (sw_box_x) and is wide enough for any rounding.
+// Backtraces that leave the staged halo read the shadow in global memory
+// instead.  Every face's arithmetic is the row kernel's (mx_face_vel4,
+// mx_backtrace, mx_face_value): the same bits.
 constexpr int kSwTX = 32, kSwTY = 8, kSwTZ = 4, kSwHA = 2, kSwThreads = kSwTX * kSwTY;
-__host__ __device__ constexpr int sw_bx(int role) { return role == 0 || role == 3 ? kSwTX + 8 : kSwTX; }
+// Box roles: 0-2 the own component for a sweep along x, y, z; 3 the axis
+// component.  First x of a box (a multiple of 4) and its width.
+__host__ __device__ constexpr int sw_box_x(int role, int x0) {
+    return (role == 0 ? x0 - 4 : (role == 3 ? x0 - 1 : x0)) & ~3;
+}
+__host__ __device__ constexpr int sw_bx(int role) {
+    return role == 0 ? kSwTX + 12 : (role == 3 ? kSwTX + 8 : kSwTX + 4);
+}
 __host__ __device__ constexpr int sw_by(int role) {
     return role == 1 ? kSwTY + 2 * kSwHA : (role == 3 ? kSwTY + 2 : kSwTY);
 }
 __host__ __device__ constexpr int sw_bz(int role) {
     return role == 2 ? kSwTZ + 2 * kSwHA : (role == 3 ? kSwTZ + 2 : kSwTZ);
 }
-constexpr int kSwOwnMax = 2048;  // floats of the largest own-component box (sweep along z)
+constexpr int kSwOwnMax = 2304;  // floats of the largest own-component box (sweep along z)
 constexpr int kSwAxCount = (kSwTX + 8) * (kSwTY + 2) * (kSwTZ + 2);
 static_assert(sw_bx(0) * sw_by(0) * sw_bz(0) <= kSwOwnMax && sw_bx(1) * sw_by(1) * sw_bz(1) <= kSwOwnMax &&
               sw_bx(2) * sw_by(2) * sw_bz(2) <= kSwOwnMax, "own box exceeds its buffer");
@@ -468,28 +483,32 @@ __device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, c
     const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
     constexpr int BX = sw_bx(AX), BY = sw_by(AX), BZ = sw_bz(AX);
     constexpr int SO = AX == 0 ? 1 : (AX == 1 ? BX : BX * BY);  // own-box stride along the sweep axis
-    constexpr int AXX = kSwTX + 8, AXY = kSwTY + 2;
+    constexpr int AXX = sw_bx(3), AXY = sw_by(3);
     // Axis-box strides along the component's axis and the sweep axis.
     constexpr int EC = C == 0 ? 1 : (C == 1 ? AXX : AXX * AXY);
     constexpr int EA = AX == 0 ? 1 : (AX == 1 ? AXX : AXX * AXY);
-    const int ox = x0 - (AX == 0 ? 4 : 0), oy = y0 - (AX == 1 ? kSwHA : 0), oz = z0 - (AX == 2 ? kSwHA : 0);
+    const int ox = sw_box_x(AX, x0), oy = y0 - (AX == 1 ? kSwHA : 0), oz = z0 - (AX == 2 ? kSwHA : 0);
     const int oa = AX == 0 ? ox : (AX == 1 ? oy : oz);  // own box's first coordinate along the axis
+    const int ax0 = sw_box_x(3, x0);
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    const int x = x0 + lx, y = y0 + ly;
+    const int y = y0 + ly;
     const int G = g.G;
-    if (x < G || x >= G + g.NX + (C == 0) || y >= G + g.NY + (C == 1)) return;
+    if (y >= G + g.NY + (C == 1)) return;
+    // The last tile of a row runs to the component's last face.
+    const int xhi = x0 + kSwTX >= G + g.NX ? G + g.NX + (C == 0) : x0 + kSwTX;
     const int zend = min(z0 + kSwTZ, G + g.NZ + (C == 2));
     const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
     const long long py = I.shp[C], pz = py * d.ny;
     const long long gs = AX == 0 ? 1 : (AX == 1 ? py : pz);
     const float dt_invh = I.dt_invh, lam = I.lam;
+    for (int x = x0 + lx; x < xhi; x += kSwTX)
     for (int z = z0; z < zend; ++z) {
         const int io = ((z - oz) * BY + (y - oy)) * BX + (x - ox);
         float vel;
         if (C == AX) {
             vel = own[io];
         } else {
-            const int ia = ((z - z0 + 1) * AXY + (y - y0 + 1)) * AXX + (x - x0 + 4);
+            const int ia = ((z - z0 + 1) * AXY + (y - y0 + 1)) * AXX + (x - ax0);
             // The row kernel's tap order: before the sweep axis's own
             // component, (-e_C, 0, e_AX - e_C, e_AX); after it,
             // (-e_C, e_AX - e_C, 0, e_AX).
@@ -519,66 +538,93 @@ __device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, c
     }
 }
 
-template <int AX, int C>
-__device__ __forceinline__ bool sweep_tile(const InstDev& I, Status* st, float* own, float* axv,
-                                           unsigned long long* bar, unsigned* ph, double* dd, int x0, int y0, int z0,
-                                           int phase) {
-    if (threadIdx.x == 0) {
-        // The previous tile's reads of the buffers (generic proxy) precede
-        // these TMA writes (async proxy).
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        constexpr unsigned own_bytes = sw_bx(AX) * sw_by(AX) * sw_bz(AX) * 4u;
-        mbar_expect_tx(bar, own_bytes + (C != AX ? kSwAxCount * 4u : 0u));
-        tma_load_3d(own, I.tmap + C * 4 + AX, x0 - (AX == 0 ? 4 : 0), y0 - (AX == 1 ? kSwHA : 0),
-                    z0 - (AX == 2 ? kSwHA : 0), bar);
-        if (C != AX) tma_load_3d(axv, I.tmap + AX * 4 + 3, x0 - 4, y0 - 1, z0 - 1, bar);
-    }
-    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *ph) ? 1 : 0) != 0;
-    *ph ^= 1u;
-    if (!ok) return false;
-    sweep_tile_faces<AX, C>(I, st, own, axv, dd, x0, y0, z0, phase);
-    return true;
+// A decoded tile of the staged sweep: slot, component and first face; dead
+// when past the work list or its slot is gated by a fault.
+struct SwTile {
+    int s, c, x0, y0, z0;
+    bool live;
+};
+
+__device__ __forceinline__ SwTile sw_decode(const InstDev* inst, const Status* st, const Tab& tab, int item, int total,
+                                            int phase) {
+    SwTile t{0, 0, 0, 0, 0, false};
+    if (item >= total) return t;
+    t.s = find_slot(tab.prefix, tab.n, item);
+    const InstDev& I = inst[t.s];
+    if (gated(&st[t.s], phase)) return t;
+    const int local = item - tab.prefix[t.s];
+    t.c = local >= I.sw_pre[2] ? 2 : (local >= I.sw_pre[1] ? 1 : 0);
+    const unsigned r = (unsigned)(local - I.sw_pre[t.c]);
+    const unsigned q1 = I.swx[t.c].div(r), q2 = I.swy[t.c].div(q1);
+    t.x0 = I.g.G + (int)(r - q1 * I.swx[t.c].d) * kSwTX;
+    t.y0 = I.g.G + (int)(q1 - q2 * I.swy[t.c].d) * kSwTY;
+    t.z0 = I.g.G + (int)q2 * kSwTZ;
+    t.live = true;
+    return t;
 }
 
+// Thread 0: the TMA loads of tile t into one buffer pair.  The buffers' last
+// reads (generic proxy) finished before the caller's barrier; the fence
+// orders them before these writes (async proxy).
+template <int AX>
+__device__ __forceinline__ void sw_issue(const InstDev& I, const SwTile& t, float* own, float* axv,
+                                         unsigned long long* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    constexpr unsigned own_bytes = sw_bx(AX) * sw_by(AX) * sw_bz(AX) * 4u;
+    mbar_expect_tx(bar, own_bytes + (t.c != AX ? kSwAxCount * 4u : 0u));
+    tma_load_3d(own, I.tmap + t.c * 4 + AX, sw_box_x(AX, t.x0), t.y0 - (AX == 1 ? kSwHA : 0),
+                t.z0 - (AX == 2 ? kSwHA : 0), bar);
+    if (t.c != AX) tma_load_3d(axv, I.tmap + AX * 4 + 3, sw_box_x(3, t.x0), t.y0 - 1, t.z0 - 1, bar);
+}
+
+// Persistent blocks walk their tiles with two buffer pairs: the loads of the
+// next tile are in flight while the current tile's faces are computed.
 template <int AX>
 __global__ void __launch_bounds__(kSwThreads, 4)
     kb_sweep_tma(const InstDev* inst, Status* st, Tab tab, int parity, int phase, unsigned* diag) {
-    __shared__ __align__(128) float own[kSwOwnMax];
-    __shared__ __align__(128) float axv[kSwAxCount];
-    __shared__ __align__(8) unsigned long long bar;
+    __shared__ __align__(128) float own[2][kSwOwnMax];
+    __shared__ __align__(128) float axv[2][kSwAxCount];
+    __shared__ __align__(8) unsigned long long bar[2];
     if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    unsigned ph = 0;
-    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
-        const int s = find_slot(tab.prefix, tab.n, item);
-        const InstDev& I = inst[s];
-        if (gated(&st[s], phase)) continue;
-        const int local = item - tab.prefix[s];
-        const int c = local >= I.sw_pre[2] ? 2 : (local >= I.sw_pre[1] ? 1 : 0);
-        const unsigned r = (unsigned)(local - I.sw_pre[c]);
-        const unsigned q1 = I.swx[c].div(r), q2 = I.swy[c].div(q1);
-        const int x0 = (I.sw_kx0 + (int)(r - q1 * I.swx[c].d)) * kSwTX;
-        const int y0 = I.g.G + (int)(q1 - q2 * I.swy[c].d) * kSwTY;
-        const int z0 = I.g.G + (int)q2 * kSwTZ;
-        double* dd = cur(I, 5 + c, parity);
-        bool ok;
-        if (c == 0) ok = sweep_tile<AX, 0>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
-        else if (c == 1) ok = sweep_tile<AX, 1>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
-        else ok = sweep_tile<AX, 2>(I, st + s, own, axv, &bar, &ph, dd, x0, y0, z0, phase);
-        if (!ok) {
-            // The transfer did not land in time: record it, give the copies in
-            // flight a second bounded wait, and stop.
-            if (threadIdx.x == 0) {
-                atomicOr(diag, 1u);
-                mbar_wait_bounded(&bar, ph ^ 1u);
+    const int total = tab.prefix[tab.n];
+    unsigned ph = 0u;  // bit k: the phase parity buffer k waits for next
+    int item = blockIdx.x, k = 0;
+    SwTile tile = sw_decode(inst, st, tab, item, total, phase);
+    if (tile.live && threadIdx.x == 0) sw_issue<AX>(inst[tile.s], tile, own[0], axv[0], &bar[0]);
+    while (item < total) {
+        const int next_item = item + gridDim.x;
+        const SwTile next = sw_decode(inst, st, tab, next_item, total, phase);
+        if (next.live && threadIdx.x == 0) sw_issue<AX>(inst[next.s], next, own[k ^ 1], axv[k ^ 1], &bar[k ^ 1]);
+        if (tile.live) {
+            const bool ok = __syncthreads_and(mbar_wait_bounded(&bar[k], (ph >> k) & 1u) ? 1 : 0) != 0;
+            ph ^= 1u << k;
+            if (!ok) {
+                // A transfer did not land in time: record it, give the copies
+                // in flight a second bounded wait, and stop.
+                if (threadIdx.x == 0) {
+                    atomicOr(diag, 1u);
+                    mbar_wait_bounded(&bar[k], ((ph >> k) & 1u) ^ 1u);
+                    if (next.live) mbar_wait_bounded(&bar[k ^ 1], (ph >> (k ^ 1)) & 1u);
+                }
+                __syncthreads();
+                return;
             }
-            __syncthreads();
-            return;
+            const InstDev& I = inst[tile.s];
+            double* dd = cur(I, 5 + tile.c, parity);
+            if (tile.c == 0) sweep_tile_faces<AX, 0>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
+            else if (tile.c == 1)
+                sweep_tile_faces<AX, 1>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
+            else sweep_tile_faces<AX, 2>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
         }
-        __syncthreads();  // every thread is done with the buffers before the next tile's loads
+        __syncthreads();  // every thread is done with buffer k before it is loaded again
+        tile = next;
+        item = next_item;
+        k ^= 1;
     }
 }
 
@@ -971,7 +1017,7 @@ __device__ float block_sum(float v, float* red) {
 // One red sweep then one black sweep of L e = r, from e_in into e_out.  The
 // red values read only e_in (their black neighbours are unchanged by the red
 // sweep); the black values read the new red values.  Each block owns an
-// output tile of TX x kPairTY x kPairTZ cells.  It first computes the new
+// output tile of TX x TY x TZ cells.  It first computes the new
 // red values of the tile plus a one-cell halo -- only the red cells, kept
 // compactly in shared memory (a row of the halo alternates colours, so
 // x >> 1 indexes its red cells) -- then, after one barrier, each lane writes
@@ -985,27 +1031,38 @@ __device__ float block_sum(float v, float* red) {
 // whose x extent leaves 1..32 cells past the last wide tile (nx = 32, 96,
 // ...) covers them with one narrow tile column (LANES = 16, TX = 32, a warp
 // per two rows) instead of a half-idle wide tile.
-constexpr int kPairTY = 16, kPairTZ = 8;
-constexpr int kPairHY = kPairTY + 2, kPairHZ = kPairTZ + 2;
+//
+// Three tile variants trade the red halo's recomputation (1.45x the tile's
+// red cells at 16 x 8 rows and planes, 1.9x at 8 x 4, 2.3x at 4 x 4) against
+// parallelism: a 64^3 level holds 32 of the largest tiles for 152 SMs.  The
+// autotuner picks a variant per level; untuned, the level's size does.
+constexpr int kPairVarTY[3] = {16, 8, 4}, kPairVarTZ[3] = {8, 4, 4};
 constexpr int kPairWideX = 64;
 
-template <int LANES>
+template <int LANES, int V>
 struct PairTile {
+    static constexpr int TY = V == 0 ? 16 : (V == 1 ? 8 : 4);
+    static constexpr int TZ = V == 0 ? 8 : 4;
+    static constexpr int HY = TY + 2, HZ = TZ + 2;
     static constexpr int TX = 2 * LANES;        // cells along x
     static constexpr int RX = LANES + 1;        // red cells of a halo row
     static constexpr int RPW = 32 / LANES;      // tile rows per warp
-    static constexpr int THREADS = kPairTY * LANES;
+    static constexpr int THREADS = TY * LANES;
+    // Resident threads per SM the launch bounds ask for: all 2048 for the
+    // largest tiles (32 registers suffice), 1536 for the others (their
+    // index arithmetic would spill at 32).
+    static constexpr int RESIDENT = V == 0 ? 2048 : 1536;
 };
 
-template <int LANES>
-__global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANES>::THREADS)
+template <int LANES, int V>
+__global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V>::RESIDENT / PairTile<LANES, V>::THREADS)
     kb_smooth_pair(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir, int vc) {
     if (vc_idle(ctl, tab.n, vc)) return;
-    using T = PairTile<LANES>;
-    __shared__ float red[kPairHZ][kPairHY][T::RX];
+    using T = PairTile<LANES, V>;
+    __shared__ float red[T::HZ][T::HY][T::RX];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = lane % LANES;                        // pair of the row
-    const int wrow = warp * T::RPW + lane / LANES;     // tile row, 0 .. kPairTY-1
+    const int wrow = warp * T::RPW + lane / LANES;     // tile row, 0 .. TY-1
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (mg_off(ctl[s], vc)) continue;
@@ -1017,15 +1074,15 @@ __global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANE
         const unsigned local = (unsigned)(item - tab.prefix[s]);
         int x0, y0, z0;
         if (LANES == 32) {
-            const unsigned q1 = L.ftx.div(local), q2 = L.fty.div(q1);
+            const unsigned q1 = L.ftx.div(local), q2 = L.fty[V].div(q1);
             x0 = (int)(local - q1 * L.ftx.d) * T::TX;
-            y0 = (int)(q1 - q2 * L.fty.d) * kPairTY;
-            z0 = (int)q2 * kPairTZ;
+            y0 = (int)(q1 - q2 * L.fty[V].d) * T::TY;
+            z0 = (int)q2 * T::TZ;
         } else {
-            const unsigned q2 = L.fty.div(local);
+            const unsigned q2 = L.fty[V].div(local);
             x0 = L.nxw;
-            y0 = (int)(local - q2 * L.fty.d) * kPairTY;
-            z0 = (int)q2 * kPairTZ;
+            y0 = (int)(local - q2 * L.fty[V].d) * T::TY;
+            z0 = (int)q2 * T::TZ;
         }
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
         // Red cells of the halo tile, a row of lanes per halo row (hy, hz):
@@ -1046,15 +1103,15 @@ __global__ void __launch_bounds__(PairTile<LANES>::THREADS, 2048 / PairTile<LANE
             }
             red[hz][hy][j] = v;
         };
-        for (int row = wrow; row < kPairHY * kPairHZ; row += kPairTY) red_row(row % kPairHY, row / kPairHY, k);
-        for (int row = tid; row < kPairHY * kPairHZ; row += T::THREADS)
-            red_row(row % kPairHY, row / kPairHY, LANES);
+        for (int row = wrow; row < T::HY * T::HZ; row += T::TY) red_row(row % T::HY, row / T::HY, k);
+        for (int row = tid; row < T::HY * T::HZ; row += T::THREADS)
+            red_row(row % T::HY, row / T::HY, LANES);
         __syncthreads();
         // Output pairs: lane k -> x = x0 + 2k + {0, 1}, tile row -> y, loop over z.
         const int y = y0 + wrow, hy = wrow + 1;
         const int xa = x0 + 2 * k;
         if (y < ny && xa < nx) {
-            const int zend = min(kPairTZ, nz - z0);
+            const int zend = min(T::TZ, nz - z0);
             int i0 = xa + nx * y + nxy * z0;
             for (int tz = 0; tz < zend; ++tz, i0 += nxy) {
                 const int z = z0 + tz, hz = tz + 1;
@@ -1371,6 +1428,7 @@ struct Batch {
     CUtensorMap* d_tmaps = nullptr;    // 12 per slot, see InstDev::tmap
     std::vector<CUtensorMap> h_tmaps;
     bool tmaps_dirty = true;
+    bool pair_chosen = false;          // the fused pairs' tile variants are set (tuned or by level size)
     unsigned* d_diag = nullptr;        // nonzero: a kernel gave up waiting on a transfer
 };
 
@@ -1462,7 +1520,7 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
         if (l >= lim || !I.lev[l].e2) return 0;
         const Lvl& L = I.lev[l];
         const long long cols = wide ? L.nxw / kPairWideX : (L.nxw < L.nx ? 1 : 0);
-        return cols * cdivl(L.ny, kPairTY) * cdivl(L.nz, kPairTZ);
+        return cols * cdivl(L.ny, kPairVarTY[sh.var]) * cdivl(L.nz, kPairVarTZ[sh.var]);
     }
     return cdivl(n, per);
 }
@@ -1549,6 +1607,29 @@ void enq_smooth(Batch* b, int st, int l, int pairs, int vc, cudaStream_t s) {
     }
 }
 
+// One fused red-black pair of level l with stage st's tile variant (wide
+// tiles for S_PAIR + l, the narrow column for S_PAIRN + l).
+template <int LANES, int V>
+void launch_pair_v(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
+    kb_smooth_pair<LANES, V><<<grid(b, st), PairTile<LANES, V>::THREADS, 0, s>>>(b->d_inst, b->d_ctl, tab(b, st), l,
+                                                                               dir, vc);
+    ++b->launches;
+}
+
+void launch_pair(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
+    const bool wide = st < S_PAIRN;
+    switch (b->shape[st].var) {
+        case 0: wide ? launch_pair_v<32, 0>(b, st, l, dir, vc, s) : launch_pair_v<16, 0>(b, st, l, dir, vc, s); break;
+        case 1: wide ? launch_pair_v<32, 1>(b, st, l, dir, vc, s) : launch_pair_v<16, 1>(b, st, l, dir, vc, s); break;
+        default: wide ? launch_pair_v<32, 2>(b, st, l, dir, vc, s) : launch_pair_v<16, 2>(b, st, l, dir, vc, s);
+    }
+}
+
+Shape pair_shape(bool wide, int var) {
+    const int threads = kPairVarTY[var] * (wide ? 32 : 16);
+    return Shape{threads, 1, (var == 0 ? 2048 : 1536) / threads, var};
+}
+
 // Pre- or post-smoothing of level l: fused pairs ping-ponging through e2
 // (an even count returns the result to e) for slots that have e2, in-place
 // colour sweeps for the others.
@@ -1556,16 +1637,8 @@ void enq_level_smooth(Batch* b, int l, int vc, cudaStream_t s) {
     // A pair reads the previous pair's output across the wide / narrow
     // boundary, so both kinds finish pair k before either starts pair k+1.
     for (int k = 0; k < b->nu; ++k) {
-        if (b->graph_pair & (1u << l)) {
-            kb_smooth_pair<32><<<grid(b, S_PAIR + l), PairTile<32>::THREADS, 0, s>>>(
-                b->d_inst, b->d_ctl, tab(b, S_PAIR + l), l, k & 1, vc);
-            ++b->launches;
-        }
-        if (b->graph_pairn & (1u << l)) {
-            kb_smooth_pair<16><<<grid(b, S_PAIRN + l), PairTile<16>::THREADS, 0, s>>>(
-                b->d_inst, b->d_ctl, tab(b, S_PAIRN + l), l, k & 1, vc);
-            ++b->launches;
-        }
+        if (b->graph_pair & (1u << l)) launch_pair(b, S_PAIR + l, l, k & 1, vc, s);
+        if (b->graph_pairn & (1u << l)) launch_pair(b, S_PAIRN + l, l, k & 1, vc, s);
     }
     if (b->graph_single & (1u << l)) enq_smooth(b, S_SMOOTH + l, l, b->nu, vc, s);
 }
@@ -1658,7 +1731,7 @@ void enq_project(Batch* b, int parity, int gate, cudaStream_t s) {
         }
     }
     LAUNCH(b, S_PBC, kb_pbc, b->d_inst, b->d_st, tab(b, S_PBC), gate);
-    LAUNCH(b, S_GRAD, kb_grad, b->d_inst, b->d_st, tab(b, S_GRAD), parity, gate);
+    LAUNCH(b, S_GRAD, kb_grad, b->d_inst, b->d_st, tab(b, S_GRAD), parity, gate, 0);
     enq_bc(b, parity, gate, s);
     rec(b, kEvProj + (gate == 3 ? 1 : 3), s);
 }
@@ -1699,8 +1772,28 @@ cudaError_t capture(Batch* b, F body, cudaGraphExec_t* out) {
     return rc;
 }
 
+// Untuned tile variants of the fused pairs, by the largest level each pair
+// stage serves: the largest tiles from 4 Mi cells, the middle ones from
+// 256 Ki, the smallest below.  Set once, before the first capture (the
+// captured kernels and the work lists must agree); the autotuner may replace
+// them.
+void default_pair_variants(Batch* b) {
+    if (b->pair_chosen || b->graph) return;
+    for (int l = 0; l < kMaxLev; ++l) {
+        long long most = 0;
+        for (const auto& S : b->slots)
+            if (S.used && l < S.d.nlev) most = std::max(most, lvl_cells(S.d.lev[l]));
+        const int var = most >= (4ll << 20) ? 0 : (most >= (256ll << 10) ? 1 : 2);
+        b->shape[S_PAIR + l] = pair_shape(true, var);
+        b->shape[S_PAIRN + l] = pair_shape(false, var);
+    }
+    b->pair_chosen = true;
+    b->tables_dirty = true;
+}
+
 cudaError_t prepare(Batch* b) {
     cudaError_t rc;
+    default_pair_variants(b);
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     const int L = max_levels(b);
     const unsigned big = big_coarse_levels(b), pair = pair_levels(b, false), pairn = pair_levels(b, true),
@@ -1812,8 +1905,8 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) {
-        b->shape[S_PAIR + l] = Shape{PairTile<32>::THREADS, 1, 2048 / PairTile<32>::THREADS};
-        b->shape[S_PAIRN + l] = Shape{PairTile<16>::THREADS, 1, 2048 / PairTile<16>::THREADS};
+        b->shape[S_PAIR + l] = pair_shape(true, 0);
+        b->shape[S_PAIRN + l] = pair_shape(false, 0);
     }
     cudaError_t rc;
     if ((rc = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -1890,7 +1983,10 @@ int plan_levels(int nx, int ny, int nz, Lvl* lev, int* coarse_sweeps) {
         L = Lvl{nx, ny, nz, wx, wy, wz, 0, 0, 0, nullptr, nullptr,
                 FastDiv((unsigned)nx), FastDiv((unsigned)ny), FastDiv((unsigned)((nx + 1) / 2)), nullptr,
                 FastDiv((unsigned)std::max(1, pair_wide_x(nx) / kPairWideX)),
-                FastDiv((unsigned)((ny + kPairTY - 1) / kPairTY)), pair_wide_x(nx)};
+                {FastDiv((unsigned)((ny + kPairVarTY[0] - 1) / kPairVarTY[0])),
+                 FastDiv((unsigned)((ny + kPairVarTY[1] - 1) / kPairVarTY[1])),
+                 FastDiv((unsigned)((ny + kPairVarTY[2] - 1) / kPairVarTY[2]))},
+                pair_wide_x(nx)};
         // An axis of extent 1 adds nothing to L e (its Neumann neighbours are
         // the cell itself, so its second difference is exactly 0); with its
         // weight kept, the relaxation would count the cell's old value as
@@ -2079,13 +2175,11 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
             acc += (int)(d.ny * d.nz * (I.shp[k] / 4));
         }
         I.shq[3] = acc;
-        // Staged sweep tiles per component: x tiles from x = 32 * (G / 32)
-        // to the component's last face, y and z tiles from G.
-        I.sw_kx0 = I.g.G / kSwTX;
+        // Staged sweep tiles per component: x, y and z tiles from G (a U
+        // row's extra face belongs to its last x tile).
         I.sw_pre[0] = 0;
         for (int k = 0; k < 3; ++k) {
-            const int xend = I.g.G + I.g.NX + (k == 0);
-            const int ntx = (xend - 1) / kSwTX - I.sw_kx0 + 1;
+            const int ntx = (I.g.NX + kSwTX - 1) / kSwTX;
             const int nty = (I.g.NY + (k == 1) + kSwTY - 1) / kSwTY;
             const int ntz = (I.g.NZ + (k == 2) + kSwTZ - 1) / kSwTZ;
             I.swx[k] = FastDiv((unsigned)ntx);
@@ -2215,6 +2309,7 @@ cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err) {
 
 cudaError_t batch_prepare_capture(Batch* b) {
     cudaError_t rc;
+    default_pair_variants(b);
     if (b->tables_dirty && (rc = upload_tables(b)) != cudaSuccess) return rc;
     if (max_levels(b) > b->graph_levels && b->graph) {
         cudaGraphExecDestroy(b->graph);
@@ -2445,12 +2540,14 @@ std::string batch_tune(Batch* b, int reps) {
         else if (st == S_DIV) kb_div<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
         else if (st == S_INT) kb_residual<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, b->d_ctl, t, 0, 0);
         else if (st == S_PBC) kb_pbc<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0);
-        else if (st == S_GRAD) kb_grad<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0);
+        else if (st == S_GRAD) kb_grad<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_st, t, 0, 0, 1);
         else if (st >= S_SMOOTH && st < S_RESTRICT) kb_smooth<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_SMOOTH, 0, 0);
         else if (st >= S_RESTRICT && st < S_PROLONG)
             kb_restrict<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_RESTRICT, 0);
         else if (st >= S_PROLONG && st < S_BIGCOARSE)
             kb_prolong<<<gsz, tpb, 0, s>>>(b->d_inst, b->d_ctl, t, st - S_PROLONG, 0);
+        else if (st >= S_PAIR && st < S_PAIRN) launch_pair(b, st, st - S_PAIR, 0, 0, s);
+        else if (st >= S_PAIRN && st < S_PAIRN + kMaxLev) launch_pair(b, st, st - S_PAIRN, 0, 0, s);
     };
     std::vector<int> stages = {S_BC, S_SHADOW, S_DIV, S_INT, S_PBC, S_GRAD};
     if (!b->tma_sweep) stages.push_back(S_SWEEP);  // the staged sweep keeps its fixed tile shape
@@ -2460,13 +2557,25 @@ std::string batch_tune(Batch* b, int reps) {
         stages.push_back(S_PROLONG + l);
     }
     bool first = true;
+    // Fused pairs: one of three tile variants per level and tile column.
+    for (int l = 0; l < L; ++l) {
+        stages.push_back(S_PAIR + l);
+        stages.push_back(S_PAIRN + l);
+    }
+    default_pair_variants(b);
+    b->pair_chosen = true;
+    const Shape pair_cands[2][3] = {{pair_shape(true, 0), pair_shape(true, 1), pair_shape(true, 2)},
+                                    {pair_shape(false, 0), pair_shape(false, 1), pair_shape(false, 2)}};
     for (int st : stages) {
         long long items = 0;
         for (auto& S : b->slots) items += stage_items(S, st, b->shape[st]);
         if (!items) continue;
         Shape best = b->shape[st];
         float best_ms = 1e30f;
-        for (const Shape& c : cands) {
+        const bool pair_st = st >= S_PAIR && st < S_PAIRN + kMaxLev;
+        std::vector<Shape> cs(cands, cands + sizeof cands / sizeof cands[0]);
+        if (pair_st) cs.assign(pair_cands[st >= S_PAIRN], pair_cands[st >= S_PAIRN] + 3);
+        for (const Shape& c : cs) {
             b->shape[st] = c;
             upload_tables(b);
             run(st);  // warm-up
@@ -2483,8 +2592,9 @@ std::string batch_tune(Batch* b, int reps) {
         }
         b->shape[st] = best;
         char buf[160];
-        snprintf(buf, sizeof buf, "%s\"stage_%d\": {\"tpb\": %d, \"ept\": %d, \"blocks_per_sm\": %d, \"us\": %.2f}",
-                 first ? "" : ", ", st, best.tpb, best.ept, best.bpsm, 1e3 * best_ms / reps);
+        snprintf(buf, sizeof buf,
+                 "%s\"stage_%d\": {\"tpb\": %d, \"ept\": %d, \"blocks_per_sm\": %d, \"variant\": %d, \"us\": %.2f}",
+                 first ? "" : ", ", st, best.tpb, best.ept, best.bpsm, best.var, 1e3 * best_ms / reps);
         report += buf;
         first = false;
     }

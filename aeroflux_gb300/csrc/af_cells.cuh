@@ -313,21 +313,28 @@ __device__ __forceinline__ void div_cell(const Geom& g, const double* __restrict
 }
 
 // --- subtractGradient, project.go:172-205 ----------------------------------
-// Face (x, y, z) of component c, inside that component's write range.
-__device__ __forceinline__ void grad_face(const Geom& g, const double* __restrict__ p, double* __restrict__ u,
-                                          double* __restrict__ v, double* __restrict__ w, double scale, int c, int x,
-                                          int y, int z) {
+// Face (x, y, z) of component c, inside that component's write range: the
+// new value of the face of f (the component's field) is stored to out at the
+// same index -- f itself for the reference's in-place update.
+__device__ __forceinline__ void grad_face_to(const Geom& g, const double* __restrict__ p, const double* f,
+                                             double* out, double scale, int c, int x, int y, int z) {
     const long long ip = x + y * g.p.sy + z * g.p.sz;
     if (c == 0) {
         const long long i = x + y * g.u.sy + z * g.u.sz;
-        u[i] = dsub(u[i], dmul(scale, dsub(p[ip], p[ip - 1])));
+        out[i] = dsub(f[i], dmul(scale, dsub(p[ip], p[ip - 1])));
     } else if (c == 1) {
         const long long i = x + y * g.v.sy + z * g.v.sz;
-        v[i] = dsub(v[i], dmul(scale, dsub(p[ip], p[ip - g.p.sy])));
+        out[i] = dsub(f[i], dmul(scale, dsub(p[ip], p[ip - g.p.sy])));
     } else {
         const long long i = x + y * g.w.sy + z * g.w.sz;
-        w[i] = dsub(w[i], dmul(scale, dsub(p[ip], p[ip - g.p.sz])));
+        out[i] = dsub(f[i], dmul(scale, dsub(p[ip], p[ip - g.p.sz])));
     }
+}
+
+__device__ __forceinline__ void grad_face(const Geom& g, const double* __restrict__ p, double* u, double* v,
+                                          double* w, double scale, int c, int x, int y, int z) {
+    double* f = c == 0 ? u : (c == 1 ? v : w);
+    grad_face_to(g, p, f, f, scale, c, x, y, z);
 }
 
 // --- binary64 <-> binary32 on the integer pipe -----------------------------

@@ -186,3 +186,26 @@ def test_benchmark_batch_reaches_tolerance():
     for s in (3, 101, 200):
         assert np.all(np.isfinite(b.download(s, "U")))
     b.close()
+
+
+def test_tuning_between_steps_leaves_the_slots_untouched():
+    # The server tunes while requests are resident: the autotuner's timing
+    # runs of every stage (the gradient included) must leave each slot's
+    # state exactly as it was.
+    cfgs = SHAPES[:4]
+    runs = []
+    for tune in (False, True):
+        b = Batch(len(cfgs))
+        slots = [b.assign(c) for c in cfgs]
+        for s in slots:
+            for n, a in zip(("U", "V", "W"), seed_fields(b.config(s), s)):
+                b.upload(s, n, a)
+        b.apply_velocity_bc()
+        b.step(2)
+        if tune:
+            b.tune(2)
+        b.step(2)
+        runs.append([np.concatenate([bits(b.download(s, n)) for n in FIELDS4]) for s in slots])
+        b.close()
+    for a, t in zip(*runs):
+        assert np.array_equal(a, t)
