@@ -1824,10 +1824,21 @@ cudaError_t prepare(Batch* b) {
     return cudaSuccess;
 }
 
-cudaError_t reset_status(Batch* b) {
+// Clears every slot's status (the step counter restarts at 0).  stop_at,
+// when given, holds per slot the Steps it performs in the coming call: a slot
+// with 0 < stop_at[s] < nsteps is gated from step stop_at[s] on -- its fault
+// gate marks the end of that step's last phase, with no fault key -- so every
+// later kernel skips it and its state stays that of its last Step.
+cudaError_t reset_status(Batch* b, const std::vector<int64_t>* stop_at = nullptr, int64_t nsteps = 0) {
     std::vector<Status> h(b->cap, Status{kNoFault, 0u, kNoKey});
+    if (stop_at)
+        for (int s = 0; s < b->cap && s < (int)stop_at->size(); ++s)
+            if ((*stop_at)[s] > 0 && (*stop_at)[s] < nsteps) h[s].fault_gate = 8u * (unsigned)(*stop_at)[s] - 1u;
     return cudaMemcpyAsync(b->d_st, h.data(), h.size() * sizeof(Status), cudaMemcpyHostToDevice, b->stream);
 }
+
+// A recorded gate without a fault key is a planned stop, not a fault.
+bool status_faulted(const Status& st) { return st.fault_gate != kNoFault && st.fault_key != kNoKey; }
 
 }  // namespace
 
@@ -2292,13 +2303,13 @@ af_field_desc batch_field(const Batch* b, int s, int field, double** dev) {
 const Geom& batch_geom(const Batch* b, int s) { return b->slots[s].d.g; }
 cudaStream_t batch_stream(Batch* b) { return b->stream; }
 
-cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err) {
+cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err, const std::vector<int64_t>* stop_at) {
     cudaError_t rc;
     if ((rc = prepare(b)) != cudaSuccess) {
         *err = std::string("aeroflux: cuda: preparing the batched step: ") + cudaGetErrorString(rc);
         return rc;
     }
-    if ((rc = reset_status(b)) != cudaSuccess) return rc;
+    if ((rc = reset_status(b, stop_at, nsteps)) != cudaSuccess) return rc;
     for (int64_t i = 0; i < nsteps; ++i)
         if ((rc = cudaGraphLaunch(b->graph, b->stream)) != cudaSuccess) {
             *err = std::string("aeroflux: cuda: cudaGraphLaunch: ") + cudaGetErrorString(rc);
@@ -2438,7 +2449,7 @@ int batch_collect_faults(Batch* b, std::string* msg, int* first_slot) {
     *first_slot = -1;
     for (int s = 0; s < b->cap; ++s) {
         SlotHost& S = b->slots[s];
-        if (!S.used || st[s].fault_gate == kNoFault) continue;
+        if (!S.used || !status_faulted(st[s])) continue;
         if (n++ == 0) {
             *first_slot = s;
             *msg = fault_message_for(S.d.g, st[s].fault_gate, st[s].fault_key);
@@ -2465,7 +2476,7 @@ bool batch_device_error(Batch* b, std::string* msg) {
 bool batch_slot_faulted(const Batch* b, int s, std::string* msg) {
     Status st;
     cudaMemcpy(&st, b->d_st + s, sizeof st, cudaMemcpyDeviceToHost);
-    if (st.fault_gate == kNoFault) return false;
+    if (!status_faulted(st)) return false;
     *msg = fault_message_for(b->slots[s].d.g, st.fault_gate, st.fault_key);
     return true;
 }
@@ -2528,6 +2539,10 @@ std::string batch_tune(Batch* b, int reps) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaStream_t s = b->stream;
+    // The control records must see the slots as they are now (a slot
+    // assigned since the last upload would read as inactive, and every
+    // multigrid stage would be timed as a no-op).
+    if (b->tables_dirty) upload_tables(b);
     kb_init<<<1, 256, 0, s>>>(b->d_inst, b->d_ctl, b->cap);
     reset_status(b);
     const int L = max_levels(b);

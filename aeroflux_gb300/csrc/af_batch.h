@@ -9,6 +9,7 @@
 #include "af_internal.h"
 
 #include <string>
+#include <vector>
 
 namespace af {
 
@@ -42,8 +43,11 @@ const Geom& batch_geom(const Batch* b, int slot);
 cudaStream_t batch_stream(Batch* b);
 
 // Enqueues one Step of every active slot on the batch stream (graph
-// replay); `nsteps` replays.  Returns a cudaError_t of the launch.
-cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err);
+// replay); `nsteps` replays.  stop_at (optional, indexed by slot) limits a
+// slot to its first stop_at[s] of them (0 or >= nsteps: all); the slot's
+// later Steps are skipped by every kernel.  Returns a cudaError_t of the
+// launch.
+cudaError_t batch_step(Batch* b, int64_t nsteps, std::string* err, const std::vector<int64_t>* stop_at = nullptr);
 // One projection (project.go:12-34) of every active slot, as a graph.
 cudaError_t batch_project(Batch* b, std::string* err);
 // A projection inside a caller's own graph (the FP64 engine's multigrid

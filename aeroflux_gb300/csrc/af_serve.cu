@@ -189,10 +189,17 @@ int af_server_round(af_server* s, int64_t* completed_now, int64_t* resident, int
         if (rc != cudaSuccess) return fail(s, AF_ERR_CUDA, cudaGetErrorString(rc));
     }
     if (!s->resident.empty()) {
-        int64_t k = s->max_round_steps;
-        for (const Req& r : s->resident) k = std::min<int64_t>(k, r.steps - r.done);
+        // A round runs up to max_round_steps Steps; a request with fewer left
+        // stops after its last one (the batch skips it for the rest of the
+        // round), so one request close to done does not shorten the round.
+        int64_t k = 0;
+        for (const Req& r : s->resident) k = std::max<int64_t>(k, r.steps - r.done);
+        k = std::min<int64_t>(k, s->max_round_steps);
+        std::vector<int64_t> stop_at(s->max_slots + 1, 0);
+        for (const Req& r : s->resident)
+            if (r.steps - r.done < k && r.slot < (int)stop_at.size()) stop_at[r.slot] = r.steps - r.done;
         std::string m;
-        cudaError_t rc = af::batch_step(s->b, k, &m);
+        cudaError_t rc = af::batch_step(s->b, k, &m, &stop_at);
         if (rc != cudaSuccess) return fail(s, AF_ERR_CUDA, m);
         cudaStreamSynchronize(af::batch_stream(s->b));
         if (af::batch_device_error(s->b, &m)) return fail(s, AF_ERR_CUDA, m);
@@ -201,8 +208,9 @@ int af_server_round(af_server* s, int64_t* completed_now, int64_t* resident, int
         const double t = s->now();
         std::vector<Req> keep;
         for (Req& r : s->resident) {
-            r.done += k;
-            s->executed_cell_steps += r.cfg.nx * r.cfg.ny * r.cfg.nz * k;
+            const int64_t ran = std::min<int64_t>(k, r.steps - r.done);
+            r.done += ran;
+            s->executed_cell_steps += r.cfg.nx * r.cfg.ny * r.cfg.nz * ran;
             std::string fm;
             const bool faulted = af::batch_slot_faulted(s->b, r.slot, &fm);
             if (faulted || r.done >= r.steps) {

@@ -113,3 +113,19 @@ def test_request_stream_summary():
     print(fp)
     assert fp["offered_requests"] == out["offered_requests"]
     assert fp["completed_requests"] + fp["censored_requests"] == fp["offered_requests"]
+
+
+def test_requests_stop_after_their_own_steps_within_longer_rounds():
+    # Rounds of up to 8 Steps while requests need 3..12: a request with fewer
+    # Steps left than the round stops after its last one and matches a
+    # standalone engine run for exactly its Steps.
+    ids, done, served, _ = serve_all(REQS, max_slots=4, round_steps=8)
+    for rid, (c, steps) in zip(ids, REQS):
+        assert done[rid]["steps"] == steps
+        e = New(c)
+        e.SeedDevice(1.0, 0.01, 42, rid)
+        e.applyVelocityBC()
+        e.Step(steps)
+        for n in ("U", "V", "W"):
+            assert np.array_equal(bits(served[rid][n]), bits(e.download(n))), f"request {rid} field {n}"
+        e.Close()
