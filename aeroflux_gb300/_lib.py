@@ -11,7 +11,10 @@ import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libaeroflux_cuda.so")
+# AEROFLUX_DEBUG_BOUNDS=1 in the environment selects the bounds-checking
+# debug build (libaeroflux_cuda_debug.so, same ABI) for this process.
+DEBUG_BOUNDS = os.environ.get("AEROFLUX_DEBUG_BOUNDS", "0") == "1"
+LIB_PATH = os.path.join(HERE, "libaeroflux_cuda_debug.so" if DEBUG_BOUNDS else "libaeroflux_cuda.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "aeroflux_cuda.h")
 
 AF_OK = 0
@@ -129,6 +132,7 @@ SIGNATURES = {
     "af_server_release": (C.c_int, [_E, C.c_int64]),
     "af_server_cancel_queued": (C.c_int, [_E, C.POINTER(C.c_int64)]),
     "af_server_get_stats": (C.c_int, [_E, C.POINTER(AfServerStats)]),
+    "af_debug_bounds": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int32]),
     "af_server_tune": (C.c_int, [_E, C.c_int32, *_ERR]),
     "af_server_destroy": (None, [_E]),
     "af_server_last_error": (C.c_char_p, [_E]),
@@ -159,7 +163,7 @@ def lib() -> C.CDLL:
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             from . import build as _build
-            _build.build()
+            _build.build(debug_bounds=DEBUG_BOUNDS)
         L = C.CDLL(LIB_PATH)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
@@ -167,3 +171,12 @@ def lib() -> C.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def debug_bounds(reset: bool = False) -> tuple[bool, int, int]:
+    """(debug build?, first violation record, violations) of the loaded library."""
+    en, first, n = C.c_int32(), C.c_uint64(), C.c_uint32()
+    rc = lib().af_debug_bounds(C.byref(en), C.byref(first), C.byref(n), int(reset))
+    if rc != AF_OK:
+        raise RuntimeError(f"af_debug_bounds failed: {rc}")
+    return bool(en.value), first.value, n.value

@@ -17,6 +17,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaeroflux_cuda.so")
+# The bounds-checking debug build: every kernel load and store checked
+# against its buffer (csrc/af_debug.cuh), same ABI, separate objects.
+BUILD_DEBUG = os.path.join(HERE, "_build_debug")
+LIB_DEBUG = os.path.join(HERE, "libaeroflux_cuda_debug.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -46,17 +50,19 @@ def _deps() -> list[str]:
     return out
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
-def _compile(unit: str, flags: list[str], verbose: bool) -> str:
+def _compile(unit: str, flags: list[str], verbose: bool, debug_bounds: bool = False) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(BUILD_DEBUG if debug_bounds else BUILD, unit.replace(".cu", ".o"))
     cmd = [nvcc(), *ARCH, *COMMON, *flags, "-c", src, "-o", obj]
+    if debug_bounds:
+        cmd.insert(1, "-DAEROFLUX_DEBUG_BOUNDS=1")
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -67,22 +73,23 @@ def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every CUDA unit for sm_103a and link the shared library."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, debug_bounds: bool = False) -> str:
+    """Compile every CUDA unit for sm_103a and link the shared library
+    (debug_bounds: the bounds-checking debug library instead)."""
+    lib = LIB_DEBUG if debug_bounds else LIB
+    if not force and up_to_date(lib):
+        return lib
+    os.makedirs(BUILD_DEBUG if debug_bounds else BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose, debug_bounds), UNITS.items()))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
-    print(LIB)
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, debug_bounds="--debug-bounds" in sys.argv))

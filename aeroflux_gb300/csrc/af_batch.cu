@@ -207,9 +207,9 @@ __global__ void kb_bc(const InstDev* inst, Status* st, Tab tab, int parity, int 
     FOR_TILES(tab)
     const InstDev& I = inst[s];
     if (gated(&st[s], gate)) continue;
-    double* u = cur(I, 1, parity);
-    double* v = cur(I, 2, parity);
-    double* w = cur(I, 3, parity);
+    AF_PTR(double) u = view(cur(I, 1, parity), I.g.u.count, DK_BC, s);
+    AF_PTR(double) v = view(cur(I, 2, parity), I.g.v.count, DK_BC, s);
+    AF_PTR(double) w = view(cur(I, 3, parity), I.g.w.count, DK_BC, s);
     const int n = I.bc_off[9];
     FOR_ELEMS(tab)
     if (el >= n) break;
@@ -234,8 +234,11 @@ __global__ void kb_div(const InstDev* inst, Status* st, Tab tab, int parity, int
     FOR_ELEMS(tab)
     if (el >= n) break;
     const unsigned e = (unsigned)el, r = I.fpx.div(e), z = I.fpy.div(r);
-    div_cell(g, cur(I, 1, parity), cur(I, 2, parity), cur(I, 3, parity), I.slot[0], I.slot[4], I.b, I.div_scale,
-             I.h2, !I.warm, (int)(e - r * g.p.nx), (int)(r - z * g.p.ny), (int)z);
+    div_cell(g, view((const double*)cur(I, 1, parity), g.u.count, DK_DIV, s),
+             view((const double*)cur(I, 2, parity), g.v.count, DK_DIV, s),
+             view((const double*)cur(I, 3, parity), g.w.count, DK_DIV, s), view(I.slot[0], g.p.count, DK_DIV, s),
+             view(I.slot[4], g.p.count, DK_DIV, s), view(I.b, g.p.count, DK_DIV, s), I.div_scale, I.h2, !I.warm,
+             (int)(e - r * g.p.nx), (int)(r - z * g.p.ny), (int)z);
     END_ELEMS
     END_TILES
 }
@@ -248,9 +251,10 @@ __global__ void kb_pbc(const InstDev* inst, Status* st, Tab tab, int gate) {
     const long long c0 = pbc_set_count(g, 0), c1 = pbc_set_count(g, 1), n = pbc_count(g);
     FOR_ELEMS(tab)
     if (el >= n) break;
-    if (el < c0) pbc_cell(g, I.slot[0], 0, el);
-    else if (el < c0 + c1) pbc_cell(g, I.slot[0], 1, el - c0);
-    else pbc_cell(g, I.slot[0], 2, el - c0 - c1);
+    AF_PTR(double) p = view(I.slot[0], g.p.count, DK_PBC, s);
+    if (el < c0) pbc_cell(g, p, 0, el);
+    else if (el < c0 + c1) pbc_cell(g, p, 1, el - c0);
+    else pbc_cell(g, p, 2, el - c0 - c1);
     END_ELEMS
     END_TILES
 }
@@ -264,9 +268,9 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
     if (gated(&st[s], gate)) continue;
     const Geom& g = I.g;
     const long long rows = 3ll * (g.NY + 1) * (g.NZ + 1);
-    double* u = cur(I, 1, parity);
-    double* v = cur(I, 2, parity);
-    double* w = cur(I, 3, parity);
+    AF_PTR(double) u = view(cur(I, 1, parity), g.u.count, DK_GRAD, s);
+    AF_PTR(double) v = view(cur(I, 2, parity), g.v.count, DK_GRAD, s);
+    AF_PTR(double) w = view(cur(I, 3, parity), g.w.count, DK_GRAD, s);
     FOR_ELEMS(tab)
     const long long row = el >> 5;
     if (row >= rows) break;
@@ -276,9 +280,11 @@ __global__ void kb_grad(const InstDev* inst, Status* st, Tab tab, int parity, in
     const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
     if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
     const int x1 = g.G + g.NX + (c == 0);
-    const double* f = c == 0 ? u : (c == 1 ? v : w);
-    double* out = scratch ? cur(I, 5 + c, parity) : (c == 0 ? u : (c == 1 ? v : w));
-    for (int x = g.G + lane; x < x1; x += 32) grad_face_to(g, I.slot[0], f, out, I.grad_scale, c, x, y, z);
+    AF_PTR(const double) f = c == 0 ? u : (c == 1 ? v : w);
+    const long long fc = c == 0 ? g.u.count : (c == 1 ? g.v.count : g.w.count);
+    AF_PTR(double) out = scratch ? view(cur(I, 5 + c, parity), fc, DK_GRAD, s) : (c == 0 ? u : (c == 1 ? v : w));
+    AF_PTR(const double) p = view((const double*)I.slot[0], g.p.count, DK_GRAD, s);
+    for (int x = g.G + lane; x < x1; x += 32) grad_face_to(g, p, f, out, I.grad_scale, c, x, y, z);
     END_ELEMS
     END_TILES
 }
@@ -300,15 +306,17 @@ __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
     const unsigned r = (unsigned)(e - I.shq[f]);
     const unsigned row = I.fsq[f].div(r), q = r - row * I.fsq[f].d;
     const Dims& d = f == 0 ? I.g.u : (f == 1 ? I.g.v : I.g.w);
-    const double* src = cur(I, 1 + f, parity) + (long long)row * d.nx + 4 * q;
-    float* dst = I.sh[f] + (long long)row * I.shp[f] + 4 * q;
+    AF_PTR(const double) src =
+        view((const double*)cur(I, 1 + f, parity), d.count, DK_SHADOW, s) + ((long long)row * d.nx + 4 * q);
+    AF_PTR(float) dst = view(I.sh[f], (long long)I.shp[f] * d.ny * d.nz, DK_SHADOW, s) +
+                        ((long long)row * I.shp[f] + 4 * q);
     const int left = d.nx - 4 * (int)q;
     float4 o;
     o.x = f64_to_f32(src[0]);
     o.y = left > 1 ? f64_to_f32(src[1]) : 0.0f;
     o.z = left > 2 ? f64_to_f32(src[2]) : 0.0f;
     o.w = left > 3 ? f64_to_f32(src[3]) : 0.0f;
-    *reinterpret_cast<float4*>(dst) = o;
+    AF_VEC(float4, dst, 0, 4) = o;
     END_ELEMS
     END_TILES
 }
@@ -321,20 +329,22 @@ __global__ void kb_shadow(const InstDev* inst, Tab tab, int parity) {
 // of that velocity's taps, so a face costs its nine loads, the arithmetic
 // of mx_face_update and one store.
 template <int AX, int C>
-__device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, double* __restrict__ dd, int y, int z,
-                                          int x0, int x1, int phase) {
+__device__ __forceinline__ void sweep_row(const InstDev& I, Status* st, AF_PTR(double) AF_RESTRICT dd, int y, int z,
+                                          int x0, int x1, int phase, int slot) {
     const Geom& g = I.g;
     const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
     const Dims& a = AX == 0 ? g.u : (AX == 1 ? g.v : g.w);
     const long long py = I.shp[C], pz = py * d.ny;  // shadow strides
-    const float* __restrict__ src = I.sh[C] + y * py + z * pz;
+    AF_PTR(const float) AF_RESTRICT src =
+        view((const float*)I.sh[C], py * d.ny * d.nz, DK_SWEEP_ROWS, slot) + (y * py + z * pz);
     dd += (long long)y * d.sy + (long long)z * d.sz;
     const long long s = AX == 0 ? 1 : (AX == 1 ? py : pz);
     const int na = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
     // Face velocity taps (summed by mx_face_vel4): offsets from (x, y, z) in the axis
     // component's shadow, in the order they are summed.
     const int ay = I.shp[AX], az = I.shp[AX] * a.ny;
-    const float* __restrict__ va = I.sh[AX] + (long long)y * ay + (long long)z * az;
+    AF_PTR(const float) AF_RESTRICT va = view((const float*)I.sh[AX], (long long)az * a.nz, DK_SWEEP_ROWS, slot) +
+                                         ((long long)y * ay + (long long)z * az);
     int o0 = 0, o1 = 0, o2 = 0, o3 = 0;
     if (C == 0 && AX == 1) { o0 = -1; o1 = 0; o2 = ay - 1; o3 = ay; }
     if (C == 0 && AX == 2) { o0 = -1; o1 = 0; o2 = az - 1; o3 = az; }
@@ -388,7 +398,8 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
         if (q >= (long long)g.NY * g.NZ) continue;
         const unsigned zz = I.fny.div((unsigned)q);
         const int y = g.G + (int)((unsigned)q - zz * (unsigned)g.NY), z = g.G + (int)zz;
-        sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, g.G + g.NX, g.G + g.NX + 1, phase);
+        sweep_row<AX, 0>(I, st + s, view(cur(I, 5, parity), g.u.count, DK_SWEEP_ROWS, s), y, z, g.G + g.NX,
+                         g.G + g.NX + 1, phase, s);
         continue;
     }
     const unsigned r = (unsigned)row, r2 = I.ffy.div(r), cc = I.ffz.div(r2);
@@ -396,9 +407,10 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
     const int y = g.G + (int)(r - r2 * (unsigned)(g.NY + 1)), z = g.G + (int)(r2 - cc * (unsigned)(g.NZ + 1));
     if (y >= g.G + g.NY + (c == 1) || z >= g.G + g.NZ + (c == 2)) continue;
     const int x0 = g.G + lane, x1 = g.G + g.NX;  // the U rows' last faces come after the rows
-    if (c == 0) sweep_row<AX, 0>(I, st + s, cur(I, 5, parity), y, z, x0, x1, phase);
-    else if (c == 1) sweep_row<AX, 1>(I, st + s, cur(I, 6, parity), y, z, x0, x1, phase);
-    else sweep_row<AX, 2>(I, st + s, cur(I, 7, parity), y, z, x0, x1, phase);
+    if (c == 0) sweep_row<AX, 0>(I, st + s, view(cur(I, 5, parity), g.u.count, DK_SWEEP_ROWS, s), y, z, x0, x1, phase, s);
+    else if (c == 1)
+        sweep_row<AX, 1>(I, st + s, view(cur(I, 6, parity), g.v.count, DK_SWEEP_ROWS, s), y, z, x0, x1, phase, s);
+    else sweep_row<AX, 2>(I, st + s, view(cur(I, 7, parity), g.w.count, DK_SWEEP_ROWS, s), y, z, x0, x1, phase, s);
     END_ELEMS
     END_TILES
 }
@@ -477,10 +489,14 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, 
 
 // Faces of one tile of component C (the loads have landed in own / axv).
 template <int AX, int C>
-__device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, const float* own, const float* axv,
-                                                 double* __restrict__ dd, int x0, int y0, int z0, int phase) {
+__device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, const float* own_, const float* axv_,
+                                                 double* __restrict__ dd_, int x0, int y0, int z0, int phase,
+                                                 int slot) {
     const Geom& g = I.g;
     const Dims& d = C == 0 ? g.u : (C == 1 ? g.v : g.w);
+    AF_PTR(const float) own = view(own_, (long long)kSwOwnMax, DK_SWEEP_TMA, slot);
+    AF_PTR(const float) axv = view(axv_, (long long)kSwAxCount, DK_SWEEP_TMA, slot);
+    AF_PTR(double) AF_RESTRICT dd = view(dd_, d.count, DK_SWEEP_TMA, slot);
     constexpr int BX = sw_bx(AX), BY = sw_by(AX), BZ = sw_bz(AX);
     constexpr int SO = AX == 0 ? 1 : (AX == 1 ? BX : BX * BY);  // own-box stride along the sweep axis
     constexpr int AXX = sw_bx(3), AXY = sw_by(3);
@@ -529,7 +545,8 @@ __device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, c
             d0 = own[io + rel * SO];
             d1 = own[io + (rel + 1) * SO];
         } else {
-            const float* gp = I.sh[C] + x + y * py + z * pz + rel * gs;
+            AF_PTR(const float) gp =
+                view((const float*)I.sh[C], pz * d.nz, DK_SWEEP_TMA, slot) + (x + y * py + z * pz + rel * gs);
             d0 = gp[0];
             d1 = gp[gs];
         }
@@ -616,10 +633,11 @@ __global__ void __launch_bounds__(kSwThreads, 4)
             }
             const InstDev& I = inst[tile.s];
             double* dd = cur(I, 5 + tile.c, parity);
-            if (tile.c == 0) sweep_tile_faces<AX, 0>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
+            if (tile.c == 0)
+                sweep_tile_faces<AX, 0>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
             else if (tile.c == 1)
-                sweep_tile_faces<AX, 1>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
-            else sweep_tile_faces<AX, 2>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase);
+                sweep_tile_faces<AX, 1>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
+            else sweep_tile_faces<AX, 2>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
         }
         __syncthreads();  // every thread is done with buffer k before it is loaded again
         tile = next;
@@ -678,10 +696,11 @@ __global__ void kb_residual(const InstDev* inst, Status* st, Ctl* ctl, Tab tab, 
             m = 0;
         }
         const Geom& g = I.g;
-        const double* __restrict__ p = I.slot[0];
-        const double* __restrict__ bb = I.b;
-        float* __restrict__ r0 = I.lev[0].r;
-        float* __restrict__ e0 = I.lev[0].e;
+        const long long nl0 = lvl_cells(I.lev[0]);
+        AF_PTR(const double) AF_RESTRICT p = view((const double*)I.slot[0], g.p.count, DK_RESIDUAL, s);
+        AF_PTR(const double) AF_RESTRICT bb = view((const double*)I.b, g.p.count, DK_RESIDUAL, s);
+        AF_PTR(float) AF_RESTRICT r0 = view(I.lev[0].r, nl0, DK_RESIDUAL, s);
+        AF_PTR(float) AF_RESTRICT e0 = view(I.lev[0].e, nl0, DK_RESIDUAL, s);
         const long long n = (long long)g.NX * g.NY * g.NZ;
         for (int k = 0; k < tab.ept; ++k) {
             const long long el = first + (long long)k * blockDim.x + threadIdx.x;
@@ -723,8 +742,10 @@ __global__ void kb_correct(const InstDev* inst, Ctl* ctl, Tab tab) {
     const int lane = (int)(el & 31);
     const unsigned zz = I.fny.div((unsigned)row);
     const int y = (int)((unsigned)row - zz * (unsigned)g.NY), z = (int)zz;
-    double* p = I.slot[0] + g.G + (long long)(g.G + y) * g.p.sy + (long long)(g.G + z) * g.p.sz;
-    const float* e = I.lev[0].e + (long long)g.NX * y + (long long)g.NX * g.NY * z;
+    AF_PTR(double) p = view(I.slot[0], g.p.count, DK_CORRECT, s) +
+                       (g.G + (long long)(g.G + y) * g.p.sy + (long long)(g.G + z) * g.p.sz);
+    AF_PTR(const float) e = view((const float*)I.lev[0].e, lvl_cells(I.lev[0]), DK_CORRECT, s) +
+                            ((long long)g.NX * y + (long long)g.NX * g.NY * z);
     for (int x = lane; x < g.NX; x += 32) p[x] += f32_to_f64(e[x]);
     END_ELEMS
     END_TILES
@@ -842,12 +863,13 @@ __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, i
     const int lane = (int)(el & 31);
     const unsigned zz = L.fny.div((unsigned)row);
     const int y = (int)((unsigned)row - zz * (unsigned)L.ny), z = (int)zz;
-    float* __restrict__ e = L.e + (long long)L.nx * y + nxy * z;
-    const float* __restrict__ rr = L.r + (long long)L.nx * y + nxy * z;
-    const float* ym = y > 0 ? e - L.nx : e;
-    const float* yp = y < L.ny - 1 ? e + L.nx : e;
-    const float* zm = z > 0 ? e - nxy : e;
-    const float* zp = z < L.nz - 1 ? e + nxy : e;
+    AF_PTR(float) AF_RESTRICT e = view(L.e, lvl_cells(L), DK_SMOOTH, s) + ((long long)L.nx * y + nxy * z);
+    AF_PTR(const float) AF_RESTRICT rr =
+        view((const float*)L.r, lvl_cells(L), DK_SMOOTH, s) + ((long long)L.nx * y + nxy * z);
+    AF_PTR(const float) ym = y > 0 ? e - L.nx : e;
+    AF_PTR(const float) yp = y < L.ny - 1 ? e + L.nx : e;
+    AF_PTR(const float) zm = z > 0 ? e - nxy : e;
+    AF_PTR(const float) zp = z < L.nz - 1 ? e + nxy : e;
     const int p = ((y + z) & 1) != color ? 1 : 0;
     for (int x = p + 2 * lane; x < L.nx; x += 64) {
         const int xm = x > 0 ? x - 1 : x, xp = x < L.nx - 1 ? x + 1 : x;
@@ -861,14 +883,16 @@ __global__ void kb_smooth(const InstDev* inst, const Ctl* ctl, Tab tab, int l, i
     END_TILES
 }
 
-__device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z) {
+__device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z, int slot) {
     const long long nxy = (long long)L.nx * L.ny;
     const long long i = lidx(x, y, z, L.nx, L.ny);
-    const float c = L.e[i];
-    const float sx = (x > 0 ? L.e[i - 1] : c) + (x < L.nx - 1 ? L.e[i + 1] : c);
-    const float sy = (y > 0 ? L.e[i - L.nx] : c) + (y < L.ny - 1 ? L.e[i + L.nx] : c);
-    const float sz = (z > 0 ? L.e[i - nxy] : c) + (z < L.nz - 1 ? L.e[i + nxy] : c);
-    return mg_res(L, sx, sy, sz, c, L.r[i]);
+    AF_PTR(const float) le = view((const float*)L.e, lvl_cells(L), DK_RESTRICT, slot);
+    AF_PTR(const float) lr = view((const float*)L.r, lvl_cells(L), DK_RESTRICT, slot);
+    const float c = le[i];
+    const float sx = (x > 0 ? le[i - 1] : c) + (x < L.nx - 1 ? le[i + 1] : c);
+    const float sy = (y > 0 ? le[i - L.nx] : c) + (y < L.ny - 1 ? le[i + L.nx] : c);
+    const float sz = (z > 0 ? le[i - nxy] : c) + (z < L.nz - 1 ? le[i + nxy] : c);
+    return mg_res(L, sx, sy, sz, c, lr[i]);
 }
 
 // Coarse rhs = mean of the children's residuals; coarse solution = 0.  One
@@ -894,8 +918,8 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l,
         // (a neighbour across a wall is the child itself); then the eight
         // residuals of mg_residual in the same order.
         const int x0 = 2 * X, y0 = 2 * Y, z0 = 2 * Z;
-        const float* b = F.e + lidx(x0, y0, z0, F.nx, F.ny);
-        const float* rb = F.r + lidx(x0, y0, z0, F.nx, F.ny);
+        AF_PTR(const float) b = view((const float*)F.e, lvl_cells(F), DK_RESTRICT, s) + lidx(x0, y0, z0, F.nx, F.ny);
+        AF_PTR(const float) rb = view((const float*)F.r, lvl_cells(F), DK_RESTRICT, s) + lidx(x0, y0, z0, F.nx, F.ny);
         const long long sy = F.nx, sz = nxy;
         float E[2][2][2], R[2][2][2];
 #pragma unroll
@@ -927,10 +951,10 @@ __global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l,
     } else {
         for (int dz = 0; dz < ez; ++dz)
             for (int dy = 0; dy < ey; ++dy)
-                for (int dx = 0; dx < ex; ++dx) sum += mg_residual(F, X * ex + dx, Y * ey + dy, Z * ez + dz);
+                for (int dx = 0; dx < ex; ++dx) sum += mg_residual(F, X * ex + dx, Y * ey + dy, Z * ez + dz, s);
     }
-    C.r[el] = sum * inv;
-    C.e[el] = 0.0f;
+    view(C.r, lvl_cells(C), DK_RESTRICT, s)[el] = sum * inv;
+    view(C.e, lvl_cells(C), DK_RESTRICT, s)[el] = 0.0f;
     END_ELEMS
     END_TILES
 }
@@ -969,11 +993,12 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
     float ay = 1.0f, az = 1.0f;
     if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
     if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
-    const float* c00 = C.e + lidx(0, Y0, Z0, C.nx, C.ny);
-    const float* c10 = C.e + lidx(0, Y1, Z0, C.nx, C.ny);
-    const float* c01 = C.e + lidx(0, Y0, Z1, C.nx, C.ny);
-    const float* c11 = C.e + lidx(0, Y1, Z1, C.nx, C.ny);
-    float* fe = F.e + lidx(0, y, z, F.nx, F.ny);
+    AF_PTR(const float) ce = view((const float*)C.e, lvl_cells(C), DK_PROLONG, s);
+    AF_PTR(const float) c00 = ce + lidx(0, Y0, Z0, C.nx, C.ny);
+    AF_PTR(const float) c10 = ce + lidx(0, Y1, Z0, C.nx, C.ny);
+    AF_PTR(const float) c01 = ce + lidx(0, Y0, Z1, C.nx, C.ny);
+    AF_PTR(const float) c11 = ce + lidx(0, Y1, Z1, C.nx, C.ny);
+    AF_PTR(float) fe = view(F.e, lvl_cells(F), DK_PROLONG, s) + lidx(0, y, z, F.nx, F.ny);
     if (F.cx) {
         // A lane owns the fine pair (2X, 2X+1): both take parent X, the even
         // one neighbour X-1 and the odd one X+1 (clamped at the walls), so
@@ -982,10 +1007,10 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
         for (int X = lane; X < C.nx; X += lanes) {
             const int Xm = max(X - 1, 0), Xp = min(X + 1, C.nx - 1);
             const float a00 = c00[X], a10 = c10[X], a01 = c01[X], a11 = c11[X];
-            float2 f = reinterpret_cast<float2*>(fe)[X];
+            float2 f = AF_VEC(float2, fe, 2 * X, 2);
             f.x = __fadd_rn(f.x, mg_interp(0.75f, ay, az, a00, c00[Xm], a10, c10[Xm], a01, c01[Xm], a11, c11[Xm]));
             f.y = __fadd_rn(f.y, mg_interp(0.75f, ay, az, a00, c00[Xp], a10, c10[Xp], a01, c01[Xp], a11, c11[Xp]));
-            reinterpret_cast<float2*>(fe)[X] = f;
+            AF_VEC(float2, fe, 2 * X, 2) = f;
         }
     } else {
         for (int x = lane; x < F.nx; x += lanes)
@@ -1067,9 +1092,9 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
         const int s = find_slot(tab.prefix, tab.n, item);
         if (mg_off(ctl[s], vc)) continue;
         const Lvl L = inst[s].lev[l];
-        const float* __restrict__ ein = dir ? L.e2 : L.e;
-        float* __restrict__ eout = dir ? L.e : L.e2;
-        const float* __restrict__ r = L.r;
+        AF_PTR(const float) AF_RESTRICT ein = view((const float*)(dir ? L.e2 : L.e), lvl_cells(L), DK_PAIR, s);
+        AF_PTR(float) AF_RESTRICT eout = view(dir ? L.e : L.e2, lvl_cells(L), DK_PAIR, s);
+        AF_PTR(const float) AF_RESTRICT r = view((const float*)L.r, lvl_cells(L), DK_PAIR, s);
         const int nx = L.nx, ny = L.ny, nz = L.nz, nxy = nx * ny;  // a level holds < 2^31 cells
         const unsigned local = (unsigned)(item - tab.prefix[s]);
         int x0, y0, z0;
@@ -1098,7 +1123,7 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
                 const int oym = y > 0 ? -nx : 0, oyp = y < ny - 1 ? nx : 0;
                 const int ozm = z > 0 ? -nxy : 0, ozp = z < nz - 1 ? nxy : 0;
                 const int oxm = x > 0 ? -1 : 0, oxp = x < nx - 1 ? 1 : 0;
-                const float* p = ein + i;
+                AF_PTR(const float) p = ein + i;
                 v = mg_relax(L, p[oxm] + p[oxp], p[oym] + p[oyp], p[ozm] + p[ozp], r[i], inv, p[0]);
             }
             red[hz][hy][j] = v;
@@ -1143,7 +1168,7 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
 // One colour: the threads walk that colour's cells only, (nx+1)/2 slots per
 // (y, z) row (the last one past the row when the row's colour count is
 // smaller), so a sweep costs half the index decoding of a walk over all cells.
-__device__ void sm_smooth(const Lvl& L, float* e, const float* r, int color) {
+__device__ void sm_smooth(const Lvl& L, AF_PTR(float) e, AF_PTR(const float) r, int color) {
     const int hx = (L.nx + 1) / 2, m = hx * L.ny * L.nz, nxy = L.nx * L.ny;
     const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
@@ -1161,7 +1186,8 @@ __device__ void sm_smooth(const Lvl& L, float* e, const float* r, int color) {
     __syncthreads();
 }
 
-__device__ __forceinline__ float sm_res(const Lvl& L, const float* e, const float* r, int x, int y, int z) {
+__device__ __forceinline__ float sm_res(const Lvl& L, AF_PTR(const float) e, AF_PTR(const float) r, int x, int y,
+                                        int z) {
     const int nxy = L.nx * L.ny;
     const int i = x + L.nx * y + nxy * z;
     const float c = e[i];
@@ -1181,21 +1207,23 @@ __global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, 
         if (mg_off(ctl[s], vc)) continue;
         const InstDev& I = inst[s];
         const int t = I.tail, nl = I.nlev;
-        float* E[kMaxLev];
-        float* R[kMaxLev];
+        AF_PTR(float) E[kMaxLev];
+        AF_PTR(float) R[kMaxLev];
         {
             float* p = tsm;
             for (int l = t; l < nl; ++l) {
                 const int n = lvl_cells(I.lev[l]);
-                E[l] = p;
-                R[l] = p + n;
+                E[l] = view(p, (long long)n, DK_VTAIL, s);
+                R[l] = view(p + n, (long long)n, DK_VTAIL, s);
                 p += 2 * n;
             }
         }
         const Lvl T = I.lev[t];
+        AF_PTR(float) te = view(T.e, lvl_cells(T), DK_VTAIL, s);
+        AF_PTR(const float) tr = view((const float*)T.r, lvl_cells(T), DK_VTAIL, s);
         for (int i = threadIdx.x; i < lvl_cells(T); i += blockDim.x) {
-            E[t][i] = T.e[i];
-            R[t][i] = T.r[i];
+            E[t][i] = te[i];
+            R[t][i] = tr[i];
         }
         __syncthreads();
         for (int l = t; l + 1 < nl; ++l) {
@@ -1249,7 +1277,7 @@ __global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, 
                 if (F.cx) { X0 = x >> 1; X1 = min(max(X0 + ((x & 1) ? 1 : -1), 0), C.nx - 1); ax = 0.75f; }
                 if (F.cy) { Y0 = y >> 1; Y1 = min(max(Y0 + ((y & 1) ? 1 : -1), 0), C.ny - 1); ay = 0.75f; }
                 if (F.cz) { Z0 = z >> 1; Z1 = min(max(Z0 + ((z & 1) ? 1 : -1), 0), C.nz - 1); az = 0.75f; }
-                const float* ec = E[l + 1];
+                AF_PTR(const float) ec = E[l + 1];
                 auto Ev = [&](int a, int b, int c) { return ec[a + C.nx * (b + C.ny * c)]; };
                 E[l][i] = __fadd_rn(E[l][i], mg_interp(ax, ay, az, Ev(X0, Y0, Z0), Ev(X1, Y0, Z0), Ev(X0, Y1, Z0),
                                                        Ev(X1, Y1, Z0), Ev(X0, Y0, Z1), Ev(X1, Y0, Z1), Ev(X0, Y1, Z1),
@@ -1261,7 +1289,7 @@ __global__ void __launch_bounds__(kCoarseThreads) kb_vtail(const InstDev* inst, 
                 sm_smooth(F, E[l], R[l], 1);
             }
         }
-        for (int i = threadIdx.x; i < lvl_cells(T); i += blockDim.x) T.e[i] = E[t][i];
+        for (int i = threadIdx.x; i < lvl_cells(T); i += blockDim.x) te[i] = E[t][i];
         __syncthreads();
     }
 }
@@ -1319,8 +1347,8 @@ __global__ void k_seed_tg(Geom g, double* u, double* v, double* w, float H, unsi
         if (comp == 0) tg = sinpif(2.0f * X) * cospif(2.0f * Y) * cospif(2.0f * Z);
         else if (comp == 1) tg = -cospif(2.0f * X) * sinpif(2.0f * Y) * cospif(2.0f * Z);
         const double val = amp * (double)tg + noise * (2.0 * uni - 1.0);
-        double* f = comp == 0 ? u : (comp == 1 ? v : w);
         const Dims& d = comp == 0 ? g.u : (comp == 1 ? g.v : g.w);
+        AF_PTR(double) f = view(comp == 0 ? u : (comp == 1 ? v : w), d.count, DK_SEED, 0);
         f[(x + g.G) + (long long)(y + g.G) * d.sy + (long long)(z + g.G) * d.sz] = val;
     }
 }
@@ -2460,6 +2488,25 @@ int batch_collect_faults(Batch* b, std::string* msg, int* first_slot) {
         b->tables_dirty = true;
     }
     return n;
+}
+
+bool batch_debug_bounds(unsigned long long* first, unsigned* count, bool reset) {
+#if AEROFLUX_DEBUG_BOUNDS
+    if (cudaMemcpyFromSymbol(first, g_dbg_first, sizeof *first) != cudaSuccess ||
+        cudaMemcpyFromSymbol(count, g_dbg_count, sizeof *count) != cudaSuccess)
+        return false;
+    if (reset) {
+        const unsigned long long none = ~0ull;
+        const unsigned zero = 0;
+        cudaMemcpyToSymbol(g_dbg_first, &none, sizeof none);
+        cudaMemcpyToSymbol(g_dbg_count, &zero, sizeof zero);
+    }
+#else
+    (void)reset;
+    *first = ~0ull;
+    *count = 0;
+#endif
+    return true;
 }
 
 bool batch_device_error(Batch* b, std::string* msg) {

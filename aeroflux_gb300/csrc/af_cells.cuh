@@ -3,6 +3,7 @@
 // cell with the same instructions.  Internal to libaeroflux_cuda.
 #pragma once
 
+#include "af_debug.cuh"
 #include "af_internal.h"
 
 #include <math.h>
@@ -191,7 +192,7 @@ __device__ __forceinline__ bool gated(const Status* st, int gate) {
 // wall face (zeroed by the first pass).  So every cell is written once from
 // cells nobody writes, and the reference's bits come out, -0 included.
 struct BcComp {
-    double* f;
+    AF_PTR(double) f;
     long long s_n, s_1, s_2;  // strides along the normal axis and the two tangential axes
     int Nn, N1, N2;           // interior extents along those axes
 };
@@ -251,7 +252,8 @@ __device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long lo
     c.f[(long long)n * c.s_n + (long long)t1 * c.s_1 + (long long)t2 * c.s_2] = val;
 }
 
-__device__ __forceinline__ BcComp bc_comp(const Geom& g, int comp, double* u, double* v, double* w) {
+__device__ __forceinline__ BcComp bc_comp(const Geom& g, int comp, AF_PTR(double) u, AF_PTR(double) v,
+                                          AF_PTR(double) w) {
     if (comp == 0) return BcComp{u, 1, g.u.sy, g.u.sz, g.NX, g.NY, g.NZ};
     if (comp == 1) return BcComp{v, g.v.sy, 1, g.v.sz, g.NY, g.NX, g.NZ};
     return BcComp{w, g.w.sz, 1, g.w.sy, g.NZ, g.NX, g.NY};
@@ -265,7 +267,7 @@ __device__ __forceinline__ long long pbc_set_count(const Geom& g, int set) {
 }
 
 // A set holds fewer than 2^32 elements: 32-bit index decoding.
-__device__ __forceinline__ void pbc_cell(const Geom& g, double* p, int set, long long il) {
+__device__ __forceinline__ void pbc_cell(const Geom& g, AF_PTR(double) p, int set, long long il) {
     const int G = g.G, NX = g.NX, NY = g.NY, NZ = g.NZ;
     const unsigned i = (unsigned)il;
     int x, y, z;
@@ -293,10 +295,11 @@ __device__ __forceinline__ void pbc_cell(const Geom& g, double* p, int set, long
 
 // --- computeDivergence (project.go:42-62) + P zeroing + B = h2*Div ---------
 // (x, y, z) is any cell of the padded P extent.
-__device__ __forceinline__ void div_cell(const Geom& g, const double* __restrict__ u, const double* __restrict__ v,
-                                         const double* __restrict__ w, double* __restrict__ p,
-                                         double* __restrict__ dv, double* __restrict__ bb, double scale, double h2,
-                                         bool zero_p, int x, int y, int z) {
+__device__ __forceinline__ void div_cell(const Geom& g, AF_PTR(const double) AF_RESTRICT u,
+                                         AF_PTR(const double) AF_RESTRICT v, AF_PTR(const double) AF_RESTRICT w,
+                                         AF_PTR(double) AF_RESTRICT p, AF_PTR(double) AF_RESTRICT dv,
+                                         AF_PTR(double) AF_RESTRICT bb, double scale, double h2, bool zero_p, int x,
+                                         int y, int z) {
     const long long i = x + y * g.p.sy + z * g.p.sz;
     if (zero_p) p[i] = 0.0;
     const int G = g.G;
@@ -316,8 +319,9 @@ __device__ __forceinline__ void div_cell(const Geom& g, const double* __restrict
 // Face (x, y, z) of component c, inside that component's write range: the
 // new value of the face of f (the component's field) is stored to out at the
 // same index -- f itself for the reference's in-place update.
-__device__ __forceinline__ void grad_face_to(const Geom& g, const double* __restrict__ p, const double* f,
-                                             double* out, double scale, int c, int x, int y, int z) {
+__device__ __forceinline__ void grad_face_to(const Geom& g, AF_PTR(const double) AF_RESTRICT p,
+                                             AF_PTR(const double) f, AF_PTR(double) out, double scale, int c, int x,
+                                             int y, int z) {
     const long long ip = x + y * g.p.sy + z * g.p.sz;
     if (c == 0) {
         const long long i = x + y * g.u.sy + z * g.u.sz;
@@ -331,9 +335,10 @@ __device__ __forceinline__ void grad_face_to(const Geom& g, const double* __rest
     }
 }
 
-__device__ __forceinline__ void grad_face(const Geom& g, const double* __restrict__ p, double* u, double* v,
-                                          double* w, double scale, int c, int x, int y, int z) {
-    double* f = c == 0 ? u : (c == 1 ? v : w);
+__device__ __forceinline__ void grad_face(const Geom& g, AF_PTR(const double) AF_RESTRICT p, AF_PTR(double) u,
+                                          AF_PTR(double) v, AF_PTR(double) w, double scale, int c, int x, int y,
+                                          int z) {
+    AF_PTR(double) f = c == 0 ? u : (c == 1 ? v : w);
     grad_face_to(g, p, f, f, scale, c, x, y, z);
 }
 
@@ -425,12 +430,12 @@ __device__ __forceinline__ float mx_face_value(float t, float d0, float d1, floa
 // New value of the face whose binary32 value sits at f[0] (its neighbours
 // along the sweep axis at f[-s] and f[s]): mx_backtrace, then mx_face_value
 // with the taps read through f.
-__device__ __forceinline__ bool mx_face_update(const float* __restrict__ f, long long s, float vel, int ca, int na,
-                                               float dt_invh, float lam, float* out) {
+__device__ __forceinline__ bool mx_face_update(AF_PTR(const float) AF_RESTRICT f, long long s, float vel, int ca,
+                                               int na, float dt_invh, float lam, float* out) {
     int i0;
     float t;
     if (!mx_backtrace(vel, ca, na, dt_invh, &i0, &t)) return false;
-    const float* p0 = f + (long long)(i0 - ca) * s;
+    AF_PTR(const float) p0 = f + (long long)(i0 - ca) * s;
     *out = mx_face_value(t, p0[0], p0[s], f[-s], f[0], f[s], lam);
     return true;
 }

@@ -7,6 +7,7 @@
 // and replayed.  Nothing is allocated per step (engine_test.go:271-288 pins
 // zero allocations per Step in the reference).
 #include "../../include/aeroflux_cuda.h"
+#include "af_debug.cuh"
 #include "af_internal.h"
 #include "af_batch.h"
 
@@ -464,6 +465,10 @@ int batch_check(af_engine* e, cudaError_t rc, const std::string& what) {
     if ((rc = cudaStreamSynchronize(af::batch_stream(e->batch))) != cudaSuccess) return cuda_fail(e, rc, "batch");
     std::string msg;
     int first = -1;
+    if (af::debug_bounds_error(&msg)) {
+        e->err = msg;
+        return AF_ERR_CUDA;
+    }
     if (af::batch_device_error(e->batch, &msg)) {
         e->err = msg;
         return AF_ERR_CUDA;
@@ -479,6 +484,7 @@ int sync_and_check(af_engine* e) {
     Status s;
     AF_CUDA(e, cudaMemcpyAsync(&s, e->st, sizeof s, cudaMemcpyDeviceToHost, e->stream));
     AF_CUDA(e, cudaStreamSynchronize(e->stream));
+    if (af::debug_bounds_error(&e->err)) return AF_ERR_CUDA;
     if (s.fault_gate != af::kNoFault) {
         e->err = fault_message(e, s.fault_gate, s.fault_key);
         // The reference returns before commitVelocity of the faulting sweep:
@@ -491,9 +497,40 @@ int sync_and_check(af_engine* e) {
 
 }  // namespace
 
+namespace af {
+
+bool debug_bounds_error(std::string* msg) {
+    unsigned long long f1 = ~0ull, f2 = ~0ull;
+    unsigned n1 = 0, n2 = 0;
+    if (!batch_debug_bounds(&f1, &n1, false) || !fp64_debug_bounds(&f2, &n2, false) || n1 + n2 == 0) return false;
+    const unsigned long long f = f1 != ~0ull ? f1 : f2;
+    *msg = sfmt("aeroflux: debug bounds check: %u out-of-buffer accesses; first in kernel %u, slot %u, at element "
+                "offset %lld",
+                n1 + n2, (unsigned)(f >> 56), (unsigned)((f >> 40) & 0xFFFF),
+                (long long)((f & 0x8000000000ull) ? (long long)(f & 0xFFFFFFFFFFull) - (1ll << 40)
+                                                  : (long long)(f & 0xFFFFFFFFFFull)));
+    batch_debug_bounds(&f1, &n1, true);
+    fp64_debug_bounds(&f2, &n2, true);
+    return true;
+}
+
+}  // namespace af
+
 extern "C" {
 
 int af_abi_version(void) { return AF_ABI_VERSION; }
+
+int af_debug_bounds(int32_t* enabled, uint64_t* first, uint32_t* violations, int32_t reset) {
+    if (!enabled || !first || !violations) return AF_ERR_ARG;
+    unsigned long long f1 = ~0ull, f2 = ~0ull;
+    unsigned n1 = 0, n2 = 0;
+    if (!af::batch_debug_bounds(&f1, &n1, reset != 0) || !af::fp64_debug_bounds(&f2, &n2, reset != 0))
+        return AF_ERR_CUDA;
+    *enabled = AEROFLUX_DEBUG_BOUNDS;
+    *first = f1 != ~0ull ? f1 : f2;
+    *violations = n1 + n2;
+    return AF_OK;
+}
 
 int af_config_normalize(af_config* cfg, char* err, size_t errlen) {
     if (!cfg) return AF_ERR_ARG;
@@ -1166,6 +1203,7 @@ int af_batch_step(af_batch* h, int64_t nsteps) {
     cudaError_t rc = af::batch_step(h->b, nsteps, &m);
     if (rc != cudaSuccess) return batch_fail(h, AF_ERR_CUDA, m);
     if (int r = batch_wait(h)) return r;
+    if (af::debug_bounds_error(&m)) return batch_fail(h, AF_ERR_CUDA, m);
     if (af::batch_device_error(h->b, &m)) return batch_fail(h, AF_ERR_CUDA, m);
     int first = -1;
     af::batch_collect_faults(h->b, &m, &first);

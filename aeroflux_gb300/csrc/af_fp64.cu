@@ -30,7 +30,8 @@ using namespace cells;
 __global__ void k_velocity_bc(Geom g, double* u, double* v, double* w, Status* st, int gate) {
     if (gated(st, gate)) return;
     const int comp = blockIdx.y / 3, set = blockIdx.y % 3;
-    const BcComp c = bc_comp(g, comp, u, v, w);
+    const BcComp c = bc_comp(g, comp, view(u, g.u.count, DK_F64_BC, 0), view(v, g.v.count, DK_F64_BC, 0),
+                             view(w, g.w.count, DK_F64_BC, 0));
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= bc_set_count(c, set)) return;
     bc_cell(c, g.G, set, i);
@@ -41,12 +42,12 @@ __global__ void k_velocity_bc(Geom g, double* u, double* v, double* w, Status* s
 // stencil.go:21-225.
 // ---------------------------------------------------------------------------
 struct SweepArgs {
-    const double* u;
-    const double* v;
-    const double* w;
-    double* tu;
-    double* tv;
-    double* tw;
+    AF_PTR(const double) u;
+    AF_PTR(const double) v;
+    AF_PTR(const double) w;
+    AF_PTR(double) tu;
+    AF_PTR(double) tv;
+    AF_PTR(double) tw;
     Dims du, dv, dw;
     int NX, NY, NZ, G;
     double dt, invH, lam;
@@ -58,9 +59,9 @@ struct SweepArgs {
 // the other two feed nothing and have no side effects.
 template <int AX>
 __device__ __forceinline__ double face_vel(const SweepArgs& a, int c, int x, int y, int z) {
-    const double* u = a.u;
-    const double* v = a.v;
-    const double* w = a.w;
+    AF_PTR(const double) u = a.u;
+    AF_PTR(const double) v = a.v;
+    AF_PTR(const double) w = a.w;
     auto U = [&](int i, int j, int k) { return u[i + j * a.du.sy + k * a.du.sz]; };
     auto V = [&](int i, int j, int k) { return v[i + j * a.dv.sy + k * a.dv.sz]; };
     auto W = [&](int i, int j, int k) { return w[i + j * a.dw.sy + k * a.dw.sz]; };
@@ -127,8 +128,8 @@ __global__ void k_sweep_fp64(SweepArgs a) {
     if (x >= x1 || y >= y1 || z >= z1) return;
 
     const Dims& d = c == 0 ? a.du : (c == 1 ? a.dv : a.dw);
-    const double* sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
-    double* dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
+    AF_PTR(const double) sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
+    AF_PTR(double) dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
 
     const double vel = face_vel<AX>(a, c, x, y, z);
     // Backtrace along the active axis only: p -= dt*v*invH.
@@ -254,9 +255,9 @@ __global__ void k_maccormack_fp64(SweepArgs a, const double* fu, const double* f
     if (x >= x1 || y >= y1 || z >= z1) return;
 
     const Dims& d = c == 0 ? a.du : (c == 1 ? a.dv : a.dw);
-    const double* sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
-    const double* fd = c == 0 ? fu : (c == 1 ? fv : fw);
-    double* dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
+    AF_PTR(const double) sd = c == 0 ? a.u : (c == 1 ? a.v : a.w);
+    AF_PTR(const double) fd = view(c == 0 ? fu : (c == 1 ? fv : fw), d.count, DK_F64_MACCORMACK, 0);
+    AF_PTR(double) dd = c == 0 ? a.tu : (c == 1 ? a.tv : a.tw);
     const long long sy = d.sy, sz = d.sz;
     const long long step = AX == 0 ? 1 : (AX == 1 ? sy : sz);
     const long long i = (long long)x + (long long)y * sy + (long long)z * sz;
@@ -308,7 +309,10 @@ __global__ void k_divergence_fp64(Geom g, const double* __restrict__ u, const do
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z;
     if (x >= g.p.nx || y >= g.p.ny) return;
-    div_cell(g, u, v, w, p, dv, bb, scale, h2, zero_p != 0, x, y, z);
+    div_cell(g, view(u, g.u.count, DK_F64_DIV, 0), view(v, g.v.count, DK_F64_DIV, 0),
+             view(w, g.w.count, DK_F64_DIV, 0), view(p, g.p.count, DK_F64_DIV, 0),
+             view(dv, g.p.count, DK_F64_DIV, 0), view(bb, g.p.count, DK_F64_DIV, 0), scale, h2, zero_p != 0, x,
+             y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -327,9 +331,11 @@ __device__ __forceinline__ double chain_add(int k, double a, double b) {
 }
 
 template <int EMU>
-__global__ void k_rbgs_fp64(Geom g, double* __restrict__ p, const double* __restrict__ bb, int color, Status* st,
-                            int gate) {
+__global__ void k_rbgs_fp64(Geom g, double* __restrict__ p_, const double* __restrict__ bb_, int color,
+                            Status* st, int gate) {
     if (gated(st, gate)) return;
+    AF_PTR(double) AF_RESTRICT p = view(p_, g.p.count, DK_F64_RBGS, 0);
+    AF_PTR(const double) AF_RESTRICT bb = view(bb_, g.p.count, DK_F64_RBGS, 0);
     const int G = g.G;
     const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int z = G + (int)blockIdx.z;
@@ -361,7 +367,7 @@ __global__ void k_pressure_bc(Geom g, double* __restrict__ p, Status* st, int ga
     const int set = blockIdx.y;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= pbc_set_count(g, set)) return;
-    pbc_cell(g, p, set, i);
+    pbc_cell(g, view(p, g.p.count, DK_F64_PBC, 0), set, i);
 }
 
 // subtractGradient, project.go:172-205.
@@ -376,15 +382,18 @@ __global__ void k_gradient_fp64(Geom g, const double* __restrict__ p, double* __
     const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int x1 = G + g.NX + (c == 0), y1 = G + g.NY + (c == 1), z1 = G + g.NZ + (c == 2);
     if (x >= x1 || y >= y1 || z >= z1) return;
-    grad_face(g, p, u, v, w, scale, c, x, y, z);
+    grad_face(g, view(p, g.p.count, DK_F64_GRAD, 0), view(u, g.u.count, DK_F64_GRAD, 0),
+              view(v, g.v.count, DK_F64_GRAD, 0), view(w, g.w.count, DK_F64_GRAD, 0), scale, c, x, y, z);
 }
 
 __global__ void k_step_tick(Status* st) { st->step += 1; }
 
 // B = h2*Div over the interior, for the red-black phase hook when Div was
 // supplied directly instead of by the divergence kernel.
-__global__ void k_b_from_div(Geom g, const double* __restrict__ dv, double* __restrict__ bb, double h2) {
+__global__ void k_b_from_div(Geom g, const double* __restrict__ dv_, double* __restrict__ bb_, double h2) {
     const int G = g.G;
+    AF_PTR(const double) AF_RESTRICT dv = view(dv_, g.p.count, DK_F64_B, 0);
+    AF_PTR(double) AF_RESTRICT bb = view(bb_, g.p.count, DK_F64_B, 0);
     const int x = G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int y = G + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int z = G + (int)blockIdx.z;
@@ -426,9 +435,12 @@ __device__ __forceinline__ void block_max_commit(unsigned long long m, unsigned 
 }
 
 // MaxDivergence, project.go:210-232.
-__global__ void k_max_divergence(Geom g, const double* __restrict__ u, const double* __restrict__ v,
-                                 const double* __restrict__ w, double invH, unsigned long long* out) {
+__global__ void k_max_divergence(Geom g, const double* __restrict__ u_, const double* __restrict__ v_,
+                                 const double* __restrict__ w_, double invH, unsigned long long* out) {
     const int G = g.G;
+    AF_PTR(const double) AF_RESTRICT u = view(u_, g.u.count, DK_F64_MAXDIV, 0);
+    AF_PTR(const double) AF_RESTRICT v = view(v_, g.v.count, DK_F64_MAXDIV, 0);
+    AF_PTR(const double) AF_RESTRICT w = view(w_, g.w.count, DK_F64_MAXDIV, 0);
     const int x = G + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int y = G + (int)blockIdx.y;
     const int z = G + (int)blockIdx.z;
@@ -445,8 +457,11 @@ __global__ void k_max_divergence(Geom g, const double* __restrict__ u, const dou
 }
 
 // MaxVelocity, stencil.go:319-331: every element of U, V, W, ghosts included.
-__global__ void k_max_abs3(const double* __restrict__ u, long long nu, const double* __restrict__ v, long long nv,
-                           const double* __restrict__ w, long long nw, unsigned long long* out) {
+__global__ void k_max_abs3(const double* __restrict__ u_, long long nu, const double* __restrict__ v_, long long nv,
+                           const double* __restrict__ w_, long long nw, unsigned long long* out) {
+    AF_PTR(const double) AF_RESTRICT u = view(u_, nu, DK_F64_MAXABS, 0);
+    AF_PTR(const double) AF_RESTRICT v = view(v_, nv, DK_F64_MAXABS, 0);
+    AF_PTR(const double) AF_RESTRICT w = view(w_, nw, DK_F64_MAXABS, 0);
     unsigned long long m = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += stride) {
@@ -484,10 +499,14 @@ __device__ __forceinline__ double block_sum_fixed(double s) {
     return s;
 }
 
-__global__ void __launch_bounds__(kKeThreads) k_ke_planes(Geom g, const double* __restrict__ u,
-                                                          const double* __restrict__ v,
-                                                          const double* __restrict__ w, double* partials) {
+__global__ void __launch_bounds__(kKeThreads) k_ke_planes(Geom g, const double* __restrict__ u_,
+                                                          const double* __restrict__ v_,
+                                                          const double* __restrict__ w_, double* partials_) {
     const int G = g.G;
+    AF_PTR(const double) AF_RESTRICT u = view(u_, g.u.count, DK_F64_KE, 0);
+    AF_PTR(const double) AF_RESTRICT v = view(v_, g.v.count, DK_F64_KE, 0);
+    AF_PTR(const double) AF_RESTRICT w = view(w_, g.w.count, DK_F64_KE, 0);
+    AF_PTR(double) partials = view(partials_, (long long)gridDim.x, DK_F64_KE, 0);
     const int z = G + (int)blockIdx.x;
     const long long n = (long long)g.NX * g.NY;
     double s = 0.0;
@@ -505,7 +524,8 @@ __global__ void __launch_bounds__(kKeThreads) k_ke_planes(Geom g, const double* 
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-__global__ void __launch_bounds__(kKeThreads) k_ke_final(const double* partials, int n, double* out) {
+__global__ void __launch_bounds__(kKeThreads) k_ke_final(const double* partials_, int n, double* out) {
+    AF_PTR(const double) partials = view(partials_, (long long)n, DK_F64_KE, 0);
     double s = 0.0;
     for (int k = threadIdx.x; k < n; k += kKeThreads) s = dadd(s, partials[k]);
     s = block_sum_fixed(s);
@@ -669,8 +689,12 @@ void launch_velocity_bc(const Geom& g, double* u, double* v, double* w, Status* 
 void launch_sweep_fp64(const Geom& g, int axis, const Fields& f, double dt, double invH, double lam, Status* st,
                        int phase, cudaStream_t s) {
     SweepArgs a;
-    a.u = f.u; a.v = f.v; a.w = f.w;
-    a.tu = f.t0; a.tv = f.t1; a.tw = f.t2;
+    a.u = view((const double*)f.u, g.u.count, DK_F64_SWEEP, 0);
+    a.v = view((const double*)f.v, g.v.count, DK_F64_SWEEP, 0);
+    a.w = view((const double*)f.w, g.w.count, DK_F64_SWEEP, 0);
+    a.tu = view(f.t0, g.u.count, DK_F64_SWEEP, 0);
+    a.tv = view(f.t1, g.v.count, DK_F64_SWEEP, 0);
+    a.tw = view(f.t2, g.w.count, DK_F64_SWEEP, 0);
     a.du = g.u; a.dv = g.v; a.dw = g.w;
     a.NX = g.NX; a.NY = g.NY; a.NZ = g.NZ; a.G = g.G;
     a.dt = dt; a.invH = invH; a.lam = lam;
@@ -687,8 +711,12 @@ void launch_maccormack_fp64(const Geom& g, int axis, const Fields& f, const Fiel
     // Forward step: the reference sweep without diffusion, into fwd.t0..t2.
     launch_sweep_fp64(g, axis, fwd, dt, invH, 0.0, st, phase, s);
     SweepArgs a;
-    a.u = f.u; a.v = f.v; a.w = f.w;
-    a.tu = f.t0; a.tv = f.t1; a.tw = f.t2;
+    a.u = view((const double*)f.u, g.u.count, DK_F64_SWEEP, 0);
+    a.v = view((const double*)f.v, g.v.count, DK_F64_SWEEP, 0);
+    a.w = view((const double*)f.w, g.w.count, DK_F64_SWEEP, 0);
+    a.tu = view(f.t0, g.u.count, DK_F64_SWEEP, 0);
+    a.tv = view(f.t1, g.v.count, DK_F64_SWEEP, 0);
+    a.tw = view(f.t2, g.w.count, DK_F64_SWEEP, 0);
     a.du = g.u; a.dv = g.v; a.dw = g.w;
     a.NX = g.NX; a.NY = g.NY; a.NZ = g.NZ; a.G = g.G;
     a.dt = dt; a.invH = invH; a.lam = lam;
@@ -766,6 +794,25 @@ void launch_max_abs3(const double* u, long long nu, const double* v, long long n
     long long n = std::max(nu, std::max(nv, nw));
     unsigned blocks = (unsigned)std::min<long long>(cdiv(n, 256), 152 * 8);
     k_max_abs3<<<blocks, 256, 0, s>>>(u, nu, v, nv, w, nw, out);
+}
+
+bool fp64_debug_bounds(unsigned long long* first, unsigned* count, bool reset) {
+#if AEROFLUX_DEBUG_BOUNDS
+    if (cudaMemcpyFromSymbol(first, g_dbg_first, sizeof *first) != cudaSuccess ||
+        cudaMemcpyFromSymbol(count, g_dbg_count, sizeof *count) != cudaSuccess)
+        return false;
+    if (reset) {
+        const unsigned long long none = ~0ull;
+        const unsigned zero = 0;
+        cudaMemcpyToSymbol(g_dbg_first, &none, sizeof none);
+        cudaMemcpyToSymbol(g_dbg_count, &zero, sizeof zero);
+    }
+#else
+    (void)reset;
+    *first = ~0ull;
+    *count = 0;
+#endif
+    return true;
 }
 
 void launch_kinetic_energy(const Geom& g, const double* u, const double* v, const double* w, double* partials,

@@ -102,6 +102,15 @@ bool selftest_div6(unsigned long long n, unsigned long long seed, unsigned long 
 // Compares the integer-pipe binary64 add and subtract with the native ones.
 bool selftest_dadd(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
 
+// Debug build (AEROFLUX_DEBUG_BOUNDS): the first out-of-buffer access each
+// kernel unit recorded -- (kernel << 56) | (slot << 40) | offset, ~0 when
+// none -- and how many there were; reset clears them.  Product build: none.
+bool fp64_debug_bounds(unsigned long long* first, unsigned* count, bool reset);
+bool batch_debug_bounds(unsigned long long* first, unsigned* count, bool reset);
+// Both units together; true with *msg set when the debug build recorded a
+// violation (the record is then cleared).
+bool debug_bounds_error(std::string* msg);
+
 // Binary64 FMA issue rate of the current device (independent chains, timed
 // with events); false on a CUDA error.
 bool measure_fp64_rate(double* fma_per_s);

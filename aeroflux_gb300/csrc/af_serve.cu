@@ -202,6 +202,7 @@ int af_server_round(af_server* s, int64_t* completed_now, int64_t* resident, int
         cudaError_t rc = af::batch_step(s->b, k, &m, &stop_at);
         if (rc != cudaSuccess) return fail(s, AF_ERR_CUDA, m);
         cudaStreamSynchronize(af::batch_stream(s->b));
+        if (af::debug_bounds_error(&m)) return fail(s, AF_ERR_CUDA, m);
         if (af::batch_device_error(s->b, &m)) return fail(s, AF_ERR_CUDA, m);
         int first = -1;
         af::batch_collect_faults(s->b, &m, &first);

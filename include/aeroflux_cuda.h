@@ -103,6 +103,16 @@ typedef enum af_field {
 
 typedef struct af_engine af_engine;
 
+/* Debug build only (no counterpart in the reference): libaeroflux_cuda_debug,
+ * built with AEROFLUX_DEBUG_BOUNDS=1, checks every device load and store of
+ * the kernels against the buffer it addresses and, instead of faulting,
+ * records the first violation -- (kernel id << 56) | (slot << 40) | element
+ * offset (40-bit two's complement) -- and counts them; the next synchronising
+ * call then fails with AF_ERR_CUDA and the location in its error text.  This
+ * reads (and with reset != 0 clears) the record: *enabled is 1 in the debug
+ * build and 0 in the product build, which records nothing. */
+int af_debug_bounds(int32_t* enabled, uint64_t* first, uint32_t* violations, int32_t reset);
+
 /* Library ABI version (AF_ABI_VERSION of the build). */
 int af_abi_version(void);
 
