@@ -119,8 +119,8 @@ struct InstDev {
     FastDiv fsq[3];          // quads per shadow row
     const CUtensorMap* tmap; // 12 tensor maps over the shadows: [component][role], role 0-2 the staged
                              // tile of a sweep along axis 0-2, role 3 the axis-velocity tile
-    int sw_pre[4];           // staged sweep: prefix of the components' tile counts
-    FastDiv swx[3], swy[3];  // staged sweep, per component: tiles along x, tiles along y
+    int sw_tiles;            // staged sweep: work items (3 components x the spatial tiles)
+    FastDiv swx, swy;        // staged sweep: spatial tiles along x and along y
     int warm;                // 1: a projection starts from the last pressure, 0: from zero
     int bc_off[10];          // velocity BC write sets: prefix of the nine (component, set) counts
     Lvl lev[kMaxLev];
@@ -569,14 +569,18 @@ __device__ __forceinline__ SwTile sw_decode(const InstDev* inst, const Status* s
     t.s = find_slot(tab.prefix, tab.n, item);
     const InstDev& I = inst[t.s];
     if (gated(&st[t.s], phase)) return t;
-    const int local = item - tab.prefix[t.s];
-    t.c = local >= I.sw_pre[2] ? 2 : (local >= I.sw_pre[1] ? 1 : 0);
-    const unsigned r = (unsigned)(local - I.sw_pre[t.c]);
-    const unsigned q1 = I.swx[t.c].div(r), q2 = I.swy[t.c].div(q1);
-    t.x0 = I.g.G + (int)(r - q1 * I.swx[t.c].d) * kSwTX;
-    t.y0 = I.g.G + (int)(q1 - q2 * I.swy[t.c].d) * kSwTY;
+    // The three components of one spatial tile are consecutive items, so
+    // the axis component's box, staged again for the other two, is still in
+    // L2.  A spatial tile past one component's last face row or plane holds
+    // no faces of it.
+    const unsigned local = (unsigned)(item - tab.prefix[t.s]);
+    const unsigned r = local / 3u;
+    t.c = (int)(local - 3u * r);
+    const unsigned q1 = I.swx.div(r), q2 = I.swy.div(q1);
+    t.x0 = I.g.G + (int)(r - q1 * I.swx.d) * kSwTX;
+    t.y0 = I.g.G + (int)(q1 - q2 * I.swy.d) * kSwTY;
     t.z0 = I.g.G + (int)q2 * kSwTZ;
-    t.live = true;
+    t.live = t.y0 < I.g.G + I.g.NY + (t.c == 1) && t.z0 < I.g.G + I.g.NZ + (t.c == 2);
     return t;
 }
 
@@ -1521,7 +1525,7 @@ long long stage_items(const SlotHost& S, int st, const Shape& sh) {
     else if (st == S_SWEEP) n = sweep_box(I.g);
     else if (st == S_GRAD) n = 32ll * 3 * (I.g.NY + 1) * (I.g.NZ + 1);
     else if (st == S_SHADOW) n = I.shq[3];
-    else if (st == S_SWEEPT) return I.sw_pre[3];
+    else if (st == S_SWEEPT) return I.sw_tiles;
     else if (st == S_DIV) n = (long long)I.g.p.nx * I.g.p.ny * I.g.p.nz;
     else if (st == S_INT) n = (long long)I.g.NX * I.g.NY * I.g.NZ;
     else if (st == S_CORR) n = 32ll * I.g.NY * I.g.NZ;
@@ -2214,17 +2218,15 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
             acc += (int)(d.ny * d.nz * (I.shp[k] / 4));
         }
         I.shq[3] = acc;
-        // Staged sweep tiles per component: x, y and z tiles from G (a U
-        // row's extra face belongs to its last x tile).
-        I.sw_pre[0] = 0;
-        for (int k = 0; k < 3; ++k) {
-            const int ntx = (I.g.NX + kSwTX - 1) / kSwTX;
-            const int nty = (I.g.NY + (k == 1) + kSwTY - 1) / kSwTY;
-            const int ntz = (I.g.NZ + (k == 2) + kSwTZ - 1) / kSwTZ;
-            I.swx[k] = FastDiv((unsigned)ntx);
-            I.swy[k] = FastDiv((unsigned)nty);
-            I.sw_pre[k + 1] = I.sw_pre[k] + ntx * nty * ntz;
-        }
+        // Staged sweep tiles: x, y and z tiles from G covering the largest
+        // component extent along each axis (a U row's extra face belongs to
+        // its last x tile), three components per spatial tile.
+        const int ntx = (I.g.NX + kSwTX - 1) / kSwTX;
+        const int nty = (I.g.NY + 1 + kSwTY - 1) / kSwTY;
+        const int ntz = (I.g.NZ + 1 + kSwTZ - 1) / kSwTZ;
+        I.swx = FastDiv((unsigned)ntx);
+        I.swy = FastDiv((unsigned)nty);
+        I.sw_tiles = 3 * ntx * nty * ntz;
     }
     size_t mg = 0;
     for (int l = 0; l < I.nlev; ++l) mg += (pair_level(l) ? 3 : 2) * (size_t)lvl_cells(I.lev[l]) * sizeof(float);
