@@ -73,6 +73,7 @@ struct Lvl {
     FastDiv ftx;            // fused-pair wide tiles along x
     FastDiv fty[3];         // fused-pair tiles along y, per tile variant (kPairVarTY)
     int nxw;                // 64 x the wide pair tiles along x; a narrow tile column covers nxw .. nx-1
+    int tma;                // 1: the level's e, e2, r have tensor maps (the TMA-staged pair may run on it)
 };
 
 struct Ctl {
@@ -117,6 +118,7 @@ struct InstDev {
     int shp[3];              // row pitch of each shadow (floats): its padded x extent rounded up to 4
     int shq[4];              // shadow conversion: prefix of the components' (row, quad) counts
     FastDiv fsq[3];          // quads per shadow row
+    const CUtensorMap* pmap; // 3 tensor maps per level for the TMA-staged pair: e, e2 and r
     const CUtensorMap* tmap; // 12 tensor maps over the shadows: [component][role], role 0-2 the staged
                              // tile of a sweep along axis 0-2, role 3 the axis-velocity tile
     int sw_tiles;            // staged sweep: work items (3 components x the spatial tiles)
@@ -473,12 +475,40 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
         : "memory");
     return ok != 0;
 }
-// Polls the barrier's phase `parity` at most kSwSpinLimit times.
+// A wait also gives up after this long (a transfer lands in microseconds).
+constexpr unsigned long long kWaitLimitNs = 200000000ull;
+// Suspend-time hint of one poll: a waiting thread sleeps in the barrier
+// until the phase completes (or this long) instead of re-issuing the poll,
+// so waiting warps take no issue slots from the working ones.
+constexpr unsigned kPollSuspendNs = 20000u;
+__device__ __forceinline__ bool mbar_try_wait_sleep(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "n"(kPollSuspendNs)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Polls the barrier's phase `parity` at most kSwSpinLimit times and for at
+// most kWaitLimitNs.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-    for (unsigned it = 0; it < kSwSpinLimit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 1; it < kSwSpinLimit; ++it) {
+        if (mbar_try_wait_sleep(bar, parity)) return true;
+        if ((it & 15u) == 0u && global_ns() - t0 > kWaitLimitNs) return false;
+    }
     return false;
 }
+// Whether an earlier kernel of the work gave up a wait (its results are
+// invalid, so later staged kernels return at once instead of waiting again).
+__device__ __forceinline__ bool diag_set(const unsigned* diag) { return *(const volatile unsigned*)diag != 0u; }
 __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z,
                                             unsigned long long* bar) {
     asm volatile(
@@ -606,12 +636,15 @@ __global__ void __launch_bounds__(kSwThreads, 4)
     __shared__ __align__(128) float own[2][kSwOwnMax];
     __shared__ __align__(128) float axv[2][kSwAxCount];
     __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ unsigned stop;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stop = diag_set(diag) ? 1u : 0u;
     }
     __syncthreads();
+    if (stop) return;
     const int total = tab.prefix[tab.n];
     unsigned ph = 0u;  // bit k: the phase parity buffer k waits for next
     int item = blockIdx.x, k = 0;
@@ -1065,7 +1098,9 @@ __device__ float block_sum(float v, float* red) {
 // red cells at 16 x 8 rows and planes, 1.9x at 8 x 4, 2.3x at 4 x 4) against
 // parallelism: a 64^3 level holds 32 of the largest tiles for 152 SMs.  The
 // autotuner picks a variant per level; untuned, the level's size does.
-constexpr int kPairVarTY[3] = {16, 8, 4}, kPairVarTZ[3] = {8, 4, 4};
+// Variant 3 is the TMA-staged z-marching pair (kb_smooth_pair_zm): 64 x 16
+// columns of 16 planes.
+constexpr int kPairVarTY[4] = {16, 8, 4, 16}, kPairVarTZ[4] = {8, 4, 4, 16};
 constexpr int kPairWideX = 64;
 
 template <int LANES, int V>
@@ -1160,6 +1195,241 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
             }
         }
         __syncthreads();
+    }
+}
+
+// --- TMA-staged, z-marching fused pair -----------------------------------------
+// The red-black pair of kb_smooth_pair on 64 x 16 columns of ZC planes,
+// marching along z with its inputs in shared-memory rings filled by TMA
+// plane loads (e_in planes of the column plus a two-cell ring, r planes plus
+// a one-cell ring).  Step k computes the red cells of halo plane z0-1+k (the
+// tile's rows plus one on each side) into a ring of red planes, then the
+// black cells of plane z0-2+k from the three red planes around it.  The red
+// halo is recomputed only across the column's sides and the chunk's two end
+// planes (1.3x the tile's red cells at ZC = 16), not around every 3-D tile.
+//
+// Walls cost no per-cell work.  The e ring holds, for the planes z0-2+p, the
+// plane clamped into the level (the plane beyond a z wall is the wall plane
+// loaded again), and once a plane lands, the cells just beyond an x or y wall
+// are overwritten with the wall cell they face.  So every neighbour of an
+// in-level red cell is read at a fixed offset and is exactly the value
+// kb_smooth_pair uses (at a wall: the cell's own).  A red position just
+// outside the level takes the old value stored there, i.e. the wall cell it
+// faces, which is the value the black cell beside it uses for its wall
+// neighbour: the black pass needs no selects either.  Arithmetic and operand
+// order are those of kb_smooth_pair: the same bits.
+//
+// Every thread keeps its rows for the whole column: warp w computes the red
+// cells of halo row w (warps 0, 1 also rows 16, 17; warp 2 the rows' 33rd
+// cells) and the black cells of tile row w.  A plane's loads are waited one
+// step before it is first read, so its wall fix-up is published by the
+// step's one block barrier.
+//
+// A level runs it only when its rows and arrays are 16-byte aligned (nx a
+// multiple of 4; InstDev::pmap, Lvl::tma).  Boxes start at x0 - 4, a 16-byte
+// boundary; box cells outside the level load as zeros and are never read.
+constexpr int kZmTX = 64, kZmTY = 16, kZmZC = 16, kZmBX = 72;
+constexpr int kZmEY = kZmTY + 4, kZmRY = kZmTY + 2;     // e rows: tile + 2 each side; r and red rows: + 1
+constexpr int kZmNE = 6, kZmNR = 5, kZmNRed = 4, kZmLead = 3, kZmNB = 4;
+constexpr int kZmEBox = kZmBX * kZmEY, kZmRBox = kZmBX * kZmRY;  // floats one plane load delivers
+// Ring slots of e and r planes start on 128-byte boundaries (the rule for a
+// TMA tensor load's shared-memory destination): plane pitches round up to 32 floats.
+constexpr int kZmEPlane = (kZmEBox + 31) / 32 * 32, kZmRPlane = (kZmRBox + 31) / 32 * 32;
+constexpr int kZmRedPlane = kZmRY * 33;
+constexpr int kZmROff = kZmNE * kZmEPlane, kZmRedOff = kZmROff + kZmNR * kZmRPlane;  // ring offsets (floats)
+constexpr int kZmFloats = kZmRedOff + kZmNRed * kZmRedPlane;
+constexpr int kZmThreads = kZmTY * 32;
+constexpr size_t kZmSmem = (size_t)kZmFloats * sizeof(float);
+// Ring sizes for a lead of kZmLead groups with each group waited one step
+// before its first read (a slot is rewritten only after its last reader).
+static_assert(kZmNE >= kZmLead + 3 && kZmNR >= kZmLead + 2 && kZmNB >= 2, "ring sizes of the z-march");
+static_assert(kZmNRed == 4, "red ring slots are taken with & 3");
+static_assert(kZmEPlane % 32 == 0 && kZmRPlane % 32 == 0 && kZmROff % 32 == 0,
+              "TMA destinations of the z-march rings on 128-byte boundaries");
+
+template <int ZC>
+__global__ void __launch_bounds__(kZmThreads, 3)
+    kb_smooth_pair_zm(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir, int vc, unsigned* diag) {
+    if (vc_idle(ctl, tab.n, vc)) return;
+    extern __shared__ __align__(128) float zsm[];
+    __shared__ __align__(8) unsigned long long bar[kZmNB];
+    __shared__ unsigned stop;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (smem_addr(zsm) & 127u) {  // the rings' TMA destinations need a 128-byte aligned base
+        if (tid == 0) atomicOr(diag, 4u);
+        return;
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kZmNB; ++i) mbar_init(&bar[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stop = diag_set(diag) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (stop) return;
+    unsigned gbase = 0;  // groups issued by this block before the current column
+    for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
+        const int s = find_slot(tab.prefix, tab.n, item);
+        if (mg_off(ctl[s], vc)) continue;
+        const Lvl L = inst[s].lev[l];
+        if (!L.tma) {  // the host switches the stage off this variant first; never stage through an unset map
+            if (tid == 0) atomicOr(diag, 2u);
+            continue;
+        }
+        AF_PTR(float) S = view(zsm, (long long)kZmFloats, DK_PAIR, s);  // the three rings
+        AF_PTR(float) AF_RESTRICT eout = view(dir ? L.e : L.e2, lvl_cells(L), DK_PAIR, s);
+        const int nx = L.nx, ny = L.ny, nz = L.nz;
+        const unsigned local = (unsigned)(item - tab.prefix[s]);
+        const unsigned q1 = L.ftx.div(local), q2 = L.fty[0].div(q1);
+        const int x0 = (int)(local - q1 * L.ftx.d) * kZmTX;
+        const int y0 = (int)(q1 - q2 * L.fty[0].d) * kZmTY;
+        const int z0 = (int)q2 * ZC;
+        const int K = min(ZC, nz - z0);  // black planes z0 .. z0+K-1; steps 0 .. K+1
+        // Group k: e plane z0+k into ring plane p = k+2 and r plane z0-1+k
+        // into r slot k % kZmNR, when needed; group 0 also brings ring
+        // planes 0 and 1 (z0-2, z0-1).  A plane just beyond a z wall loads
+        // the wall plane; one further out is never read and not loaded.
+        auto issue = [&](int k) {
+            const unsigned g = gbase + (unsigned)k;
+            unsigned long long* b = &bar[g % kZmNB];
+            const int pa = k == 0 ? 0 : k + 2, pb = k + 2;
+            int ne = 0;
+            for (int p = pa; p <= pb; ++p) ne += (z0 - 2 + p >= -1 && z0 - 2 + p <= nz) ? 1 : 0;
+            const int rz = z0 - 1 + k;
+            const bool rr = rz >= 0 && rz < nz;
+            mbar_expect_tx(b, (unsigned)((ne * kZmEBox + (rr ? kZmRBox : 0)) * sizeof(float)));
+            const CUtensorMap* em = inst[s].pmap + 3 * l + dir;
+            for (int p = pa; p <= pb; ++p) {
+                const int z = z0 - 2 + p;
+                if (z >= -1 && z <= nz)
+                    tma_load_3d(zsm + (p % kZmNE) * kZmEPlane, em, x0 - 4, y0 - 2, min(max(z, 0), nz - 1), b);
+            }
+            if (rr)
+                tma_load_3d(zsm + kZmROff + (k % kZmNR) * kZmRPlane, inst[s].pmap + 3 * l + 2, x0 - 4, y0 - 1, rz, b);
+        };
+        // Wall fix-up of a landed e plane: the cell beyond an x or y wall
+        // takes the wall cell's value (box column 4 is x = x0, box row 2 is
+        // y = y0).  Only cells beside an in-level cell matter; the corners
+        // two walls share are never read.
+        const int wx0 = x0 == 0, wx1 = x0 + kZmTX >= nx, wy0 = y0 == 0, wy1 = y0 + kZmRY - 1 >= ny;
+        const bool walls = wx0 | wx1 | wy0 | wy1;
+        const int gx = nx - x0 + 4, gy = ny - y0 + 2;  // box column of x = nx, box row of y = ny
+        auto fill = [&](int slot) {
+            AF_PTR(float) P = S + slot * kZmEPlane;
+            if (tid < kZmEY) {
+                if (wx0) P[tid * kZmBX + 3] = P[tid * kZmBX + 4];
+                if (wx1) P[tid * kZmBX + gx] = P[tid * kZmBX + gx - 1];
+            } else if (tid >= 32 && tid < 32 + kZmBX) {
+                const int c = tid - 32;
+                if (wy0) P[kZmBX + c] = P[2 * kZmBX + c];
+                if (wy1) P[gy * kZmBX + c] = P[(gy - 1) * kZmBX + c];
+            }
+        };
+        const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
+        // Red rows of this thread: halo row `warp` at cell `lane`, and an
+        // extra one (rows 16, 17 at cell lane for warps 0, 1; cell 32 of row
+        // lane for warp 2).  e box offset of the cell for parity 0, red
+        // offset, level row and level x of the cell for parity 0.
+        const int xe = warp < kZmRY - kZmTY ? 1 : (warp == kZmRY - kZmTY && lane < kZmRY ? 2 : 0);
+        const int hyB = xe == 1 ? kZmTY + warp : (xe == 2 ? lane : 0), jB = xe == 2 ? 32 : lane;
+        const int eA = (warp + 1) * kZmBX + 3 + 2 * lane, eB = (hyB + 1) * kZmBX + 3 + 2 * jB;
+        const int dA = warp * 33 + lane, dB = hyB * 33 + jB;
+        const int yA = y0 - 1 + warp, yB = y0 - 1 + hyB;
+        const int xA = x0 - 1 + 2 * lane, xB = x0 - 1 + 2 * jB;
+        // Black cells of this thread: tile row `warp`, pair x0 + 2 lane, +1.
+        const int by = y0 + warp;
+        const bool bok = by < ny && x0 + 2 * lane < nx;
+        const int ebk = (warp + 2) * kZmBX + 2 * lane + 5;  // e box offset of the black cell when the pair starts red
+        const int rbk = kZmRedOff + (warp + 1) * 33 + lane;  // red offset of cell lane in halo row warp+1
+        const long long nxy = (long long)nx * ny;
+        AF_PTR(float) gp = eout + ((long long)(x0 + 2 * lane) + (long long)nx * by + nxy * z0);
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (int k = 0; k < kZmLead && k <= K + 1; ++k) issue(k);
+        }
+        auto give_up = [&](int first, int last) {  // tid 0: let the transfers of groups first..last land
+            for (int j = first; j <= last && j <= K + 1; ++j) {
+                const unsigned gj = gbase + (unsigned)j;
+                mbar_wait_bounded(&bar[gj % kZmNB], (gj / kZmNB) & 1u);
+            }
+        };
+        bool failed = !mbar_wait_bounded(&bar[gbase % kZmNB], (gbase / kZmNB) & 1u);
+        if (walls && !failed) {
+            fill(0);
+            fill(1);
+            fill(2);
+        }
+        if (__syncthreads_or(failed ? 1 : 0)) {
+            if (tid == 0) {
+                atomicOr(diag, 1u);
+                give_up(0, kZmLead - 1);
+            }
+            __syncthreads();
+            return;
+        }
+        int s0 = 0, s1 = 1, s2 = 2, s3 = 3;  // e ring slots of planes k .. k+3
+        int sr = 0, srp = kZmNR - 1;         // r ring slots of planes k, k-1
+        for (int k = 0; k <= K + 1; ++k) {
+            if (k + 1 <= K + 1) {  // group k+1, first read at step k+1
+                const unsigned g = gbase + (unsigned)(k + 1);
+                if (!failed && !mbar_wait_bounded(&bar[g % kZmNB], (g / kZmNB) & 1u)) failed = true;
+                if (walls && !failed) fill(s3);
+            }
+            const int zr = z0 - 1 + k;
+            const int zin = (unsigned)zr < (unsigned)nz ? 1 : 0;
+            const int ec = s1 * kZmEPlane, dzm = (s0 - s1) * kZmEPlane, dzp = (s2 - s1) * kZmEPlane;
+            const int drr = kZmROff + sr * kZmRPlane - ec - kZmBX;  // r cell of e offset b (r rows start one lower)
+            const int rs = kZmRedOff + (k & 3) * kZmRedPlane;
+            if (!failed) {
+                auto red_cell = [&](int e0, int d0, int y, int x) {
+                    const int par = (y + zr + 1) & 1;
+                    const int b = ec + e0 + par;
+                    const bool in = zin && (unsigned)y < (unsigned)ny && (unsigned)(x + par) < (unsigned)nx;
+                    const float c = S[b];
+                    S[rs + d0] = in ? mg_relax(L, S[b - 1] + S[b + 1], S[b - kZmBX] + S[b + kZmBX],
+                                               S[b + dzm] + S[b + dzp], S[b + drr], inv, c)
+                                    : c;
+                };
+                red_cell(eA, dA, yA, xA);
+                if (xe) red_cell(eB, dB, yB, xB);
+            }
+            if (__syncthreads_or(failed ? 1 : 0)) {
+                if (tid == 0) {
+                    atomicOr(diag, 1u);
+                    give_up(k + 1, k + kZmLead - 1);
+                }
+                __syncthreads();
+                return;
+            }
+            if (tid == 0 && k + kZmLead <= K + 1) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(k + kZmLead);
+            }
+            if (k >= 2 && bok) {
+                // Black cells of plane zr - 1: e ring plane k, r plane k-1,
+                // red planes k-2, k-1, k.
+                const int pr = (by + zr - 1) & 1;
+                const int eb = s0 * kZmEPlane + ebk - pr;
+                const float c = S[eb];
+                const float rv = S[kZmROff + srp * kZmRPlane + ebk - kZmBX - pr];
+                const int r1 = rbk + ((k - 1) & 3) * kZmRedPlane;
+                const int q = 1 - pr;
+                const float sx = S[r1] + S[r1 + 1];
+                const float sy = S[r1 + q - 33] + S[r1 + q + 33];
+                const float sz = S[rbk + ((k - 2) & 3) * kZmRedPlane + q] + S[rbk + (k & 3) * kZmRedPlane + q];
+                const float bv = mg_relax(L, sx, sy, sz, rv, inv, c);
+                const float red_v = S[r1 + pr];
+                AF_VEC(float2, gp, 0, 2) = pr ? make_float2(bv, red_v) : make_float2(red_v, bv);
+            }
+            if (k >= 2) gp += nxy;
+            s0 = s1;
+            s1 = s2;
+            s2 = s3;
+            s3 = s3 + 1 == kZmNE ? 0 : s3 + 1;
+            srp = sr;
+            sr = sr + 1 == kZmNR ? 0 : sr + 1;
+        }
+        gbase += (unsigned)(K + 2);
+        __syncthreads();  // every thread is done with the rings before the next column's loads
     }
 }
 
@@ -1460,6 +1730,9 @@ struct Batch {
     CUtensorMap* d_tmaps = nullptr;    // 12 per slot, see InstDev::tmap
     std::vector<CUtensorMap> h_tmaps;
     bool tmaps_dirty = true;
+    CUtensorMap* d_pmaps = nullptr;    // 3 per level and slot, see InstDev::pmap
+    std::vector<CUtensorMap> h_pmaps;
+    int force_pair_var = -1;           // AEROFLUX_PAIR_VARIANT: every fused pair stage's variant (-1: tuned)
     bool pair_chosen = false;          // the fused pairs' tile variants are set (tuned or by level size)
     unsigned* d_diag = nullptr;        // nonzero: a kernel gave up waiting on a transfer
 };
@@ -1583,6 +1856,8 @@ cudaError_t upload_tables(Batch* b) {
         return rc;
     if (b->tmaps_dirty) {
         if ((rc = cudaMemcpyAsync(b->d_tmaps, b->h_tmaps.data(), b->h_tmaps.size() * sizeof(CUtensorMap),
+                                  cudaMemcpyHostToDevice, b->stream)) != cudaSuccess ||
+            (rc = cudaMemcpyAsync(b->d_pmaps, b->h_pmaps.data(), b->h_pmaps.size() * sizeof(CUtensorMap),
                                   cudaMemcpyHostToDevice, b->stream)) != cudaSuccess)
             return rc;
         b->tmaps_dirty = false;
@@ -1650,6 +1925,12 @@ void launch_pair_v(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
 
 void launch_pair(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
     const bool wide = st < S_PAIRN;
+    if (wide && b->shape[st].var == 3) {
+        kb_smooth_pair_zm<kZmZC><<<grid(b, st), kZmThreads, kZmSmem, s>>>(b->d_inst, b->d_ctl, tab(b, st), l, dir,
+                                                                         vc, b->d_diag);
+        ++b->launches;
+        return;
+    }
     switch (b->shape[st].var) {
         case 0: wide ? launch_pair_v<32, 0>(b, st, l, dir, vc, s) : launch_pair_v<16, 0>(b, st, l, dir, vc, s); break;
         case 1: wide ? launch_pair_v<32, 1>(b, st, l, dir, vc, s) : launch_pair_v<16, 1>(b, st, l, dir, vc, s); break;
@@ -1658,8 +1939,31 @@ void launch_pair(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
 }
 
 Shape pair_shape(bool wide, int var) {
+    if (var == 3) return Shape{kZmThreads, 1, 3, 3};  // shared memory holds three z-marching blocks per SM
     const int threads = kPairVarTY[var] * (wide ? 32 : 16);
     return Shape{threads, 1, (var == 0 ? 2048 : 1536) / threads, var};
+}
+
+// Whether a used slot has wide pair tiles at level l without the staged
+// pair's maps.
+bool pair_tma_missing(const Batch* b, int l) {
+    for (const auto& S : b->slots)
+        if (S.used && l < S.d.nlev && S.d.lev[l].e2 && S.d.lev[l].nxw > 0 && !S.d.lev[l].tma) return true;
+    return false;
+}
+
+// Whether every used slot whose level l has wide pair tiles can run the
+// TMA-staged pair there (and at least one has them).
+bool pair_tma_ok(const Batch* b, int l) {
+    bool any = false;
+    for (const auto& S : b->slots) {
+        if (!S.used || l >= S.d.nlev) continue;
+        const Lvl& L = S.d.lev[l];
+        if (!L.e2 || L.nxw == 0) continue;
+        if (!L.tma) return false;
+        any = true;
+    }
+    return any;
 }
 
 // Pre- or post-smoothing of level l: fused pairs ping-ponging through e2
@@ -1810,14 +2114,26 @@ cudaError_t capture(Batch* b, F body, cudaGraphExec_t* out) {
 // captured kernels and the work lists must agree); the autotuner may replace
 // them.
 void default_pair_variants(Batch* b) {
+    // A slot assigned after the choice may lack the staged pair's maps at a
+    // level that runs it: that level goes back to the plain variant 1 tiles.
+    for (int l = 0; l < kMaxLev; ++l)
+        if (b->shape[S_PAIR + l].var == 3 && pair_tma_missing(b, l)) {
+            b->shape[S_PAIR + l] = pair_shape(true, 1);
+            b->tables_dirty = true;
+            if (b->graph) {
+                cudaGraphExecDestroy(b->graph);
+                b->graph = nullptr;
+            }
+        }
     if (b->pair_chosen || b->graph) return;
     for (int l = 0; l < kMaxLev; ++l) {
         long long most = 0;
         for (const auto& S : b->slots)
             if (S.used && l < S.d.nlev) most = std::max(most, lvl_cells(S.d.lev[l]));
-        const int var = most >= (4ll << 20) ? 0 : (most >= (256ll << 10) ? 1 : 2);
-        b->shape[S_PAIR + l] = pair_shape(true, var);
-        b->shape[S_PAIRN + l] = pair_shape(false, var);
+        int var = most >= (4ll << 20) ? 0 : (most >= (256ll << 10) ? 1 : 2);
+        if (b->force_pair_var >= 0) var = b->force_pair_var;
+        b->shape[S_PAIR + l] = pair_shape(true, var == 3 && !pair_tma_ok(b, l) ? 1 : var);
+        b->shape[S_PAIRN + l] = pair_shape(false, var == 3 ? 1 : var);
     }
     b->pair_chosen = true;
     b->tables_dirty = true;
@@ -1918,6 +2234,32 @@ bool encode_slot_maps(const InstDev& I, CUtensorMap* maps) {
     return true;
 }
 
+// The three tensor maps of the z-marching pair per level (e, e2, r: one
+// plane of a 64 x 16 column plus a two-cell ring for e and e2, a one-cell
+// ring for r) for every level with wide pair tiles whose rows and arrays are
+// 16-byte aligned; sets Lvl::tma on those levels.
+void encode_pair_maps(InstDev& I, CUtensorMap* maps) {
+    auto enc = tensor_map_encoder();
+    for (int l = 0; l < I.nlev; ++l) {
+        Lvl& L = I.lev[l];
+        L.tma = 0;
+        if (!enc || !L.e2 || L.nxw == 0 || L.nx % 4 != 0) continue;
+        auto aligned = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+        if (!aligned(L.e) || !aligned(L.e2) || !aligned(L.r)) continue;
+        const cuuint64_t dims[3] = {(cuuint64_t)L.nx, (cuuint64_t)L.ny, (cuuint64_t)L.nz};
+        const cuuint64_t strides[2] = {(cuuint64_t)L.nx * 4u, (cuuint64_t)L.nx * L.ny * 4u};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const cuuint32_t ebox[3] = {kZmBX, kZmEY, 1}, rbox[3] = {kZmBX, kZmRY, 1};
+        float* arr[3] = {L.e, L.e2, L.r};
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; ++k)
+            ok = enc(&maps[3 * l + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, arr[k], dims, strides, k < 2 ? ebox : rbox,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        L.tma = ok ? 1 : 0;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1959,6 +2301,7 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
         (rc = cudaMalloc(&b->d_ctl, sizeof(Ctl) * (capacity + 1))) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_tab, sizeof(int) * (size_t)S_COUNT * (capacity + 1))) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_tmaps, sizeof(CUtensorMap) * 12 * (size_t)capacity)) != cudaSuccess ||
+        (rc = cudaMalloc(&b->d_pmaps, sizeof(CUtensorMap) * 3 * kMaxLev * (size_t)capacity)) != cudaSuccess ||
         (rc = cudaMalloc(&b->d_diag, sizeof(unsigned))) != cudaSuccess) {
         *err = std::string("aeroflux: batch tables: ") + cudaGetErrorString(rc);
         batch_destroy(b);
@@ -1967,6 +2310,11 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl) * (capacity + 1), b->stream);
     cudaMemsetAsync(b->d_diag, 0, sizeof(unsigned), b->stream);
     b->h_tmaps.assign(12 * (size_t)capacity, CUtensorMap{});
+    b->h_pmaps.assign(3 * kMaxLev * (size_t)capacity, CUtensorMap{});
+    cudaFuncSetAttribute(kb_smooth_pair_zm<kZmZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZmSmem);
+    // The fused pairs' tile variant for every level (0-2; 3: TMA-staged where
+    // the levels allow it), instead of the tuned or size-based choice.
+    if (const char* pv = getenv("AEROFLUX_PAIR_VARIANT")) b->force_pair_var = std::min(3, std::max(0, atoi(pv)));
     if (pool_bytes) {
         if (!b->pool.init(pool_bytes)) {
             *err = "aeroflux: batch device pool of " + std::to_string(pool_bytes) + " bytes: out of memory";
@@ -1997,6 +2345,7 @@ void batch_destroy(Batch* b) {
     cudaFree(b->d_ctl);
     cudaFree(b->d_tab);
     cudaFree(b->d_tmaps);
+    cudaFree(b->d_pmaps);
     cudaFree(b->d_diag);
     if (b->body) cudaStreamDestroy(b->body);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -2283,6 +2632,8 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
         }
     }
     cudaMemsetAsync(p, 0, mg, b->stream);
+    I.pmap = b->d_pmaps + 3 * kMaxLev * (size_t)s;
+    encode_pair_maps(I, &b->h_pmaps[3 * kMaxLev * (size_t)s]);
     const double half = c.dt * 0.5;  // aeroflux.go:353
     const double invH = 1.0 / c.h;
     I.dt_invh = (float)(half * invH);
@@ -2517,8 +2868,12 @@ bool batch_device_error(Batch* b, std::string* msg) {
     cudaMemcpy(&v, b->d_diag, sizeof v, cudaMemcpyDeviceToHost);
     if (!v) return false;
     cudaMemset(b->d_diag, 0, sizeof v);
-    *msg = "aeroflux: cuda: a staged-sweep kernel gave up waiting for its tile transfer; the step's results are "
-           "invalid";
+    *msg = (v & 4u)   ? "aeroflux: cuda: the staged pair's shared-memory rings are not 128-byte aligned; the step's "
+                        "results are invalid"
+           : (v & 2u) ? "aeroflux: cuda: the TMA-staged pair ran on a level without tensor maps; the step's results "
+                        "are invalid"
+                      : "aeroflux: cuda: a staged kernel gave up waiting for its tile transfer; the step's results "
+                        "are invalid";
     return true;
 }
 
@@ -2637,8 +2992,13 @@ std::string batch_tune(Batch* b, int reps) {
         Shape best = b->shape[st];
         float best_ms = 1e30f;
         const bool pair_st = st >= S_PAIR && st < S_PAIRN + kMaxLev;
+        if (pair_st && b->force_pair_var >= 0) continue;
         std::vector<Shape> cs(cands, cands + sizeof cands / sizeof cands[0]);
-        if (pair_st) cs.assign(pair_cands[st >= S_PAIRN], pair_cands[st >= S_PAIRN] + 3);
+        if (pair_st) {
+            cs.assign(pair_cands[st >= S_PAIRN], pair_cands[st >= S_PAIRN] + 3);
+            if (st < S_PAIRN && pair_tma_ok(b, st - S_PAIR)) cs.push_back(pair_shape(true, 3));
+        }
+        std::string tried;  // fused-pair stages: every tile variant's time
         for (const Shape& c : cs) {
             b->shape[st] = c;
             upload_tables(b);
@@ -2649,17 +3009,25 @@ std::string batch_tune(Batch* b, int reps) {
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (cudaGetLastError() == cudaSuccess && ms < best_ms) {
+            const bool ok = cudaGetLastError() == cudaSuccess;
+            if (ok && ms < best_ms) {
                 best_ms = ms;
                 best = c;
+            }
+            if (pair_st) {
+                char t[48];
+                snprintf(t, sizeof t, "%s\"%d\": %.2f", tried.empty() ? "" : ", ", c.var, ok ? 1e3 * ms / reps : -1.0);
+                tried += t;
             }
         }
         b->shape[st] = best;
         char buf[160];
         snprintf(buf, sizeof buf,
-                 "%s\"stage_%d\": {\"tpb\": %d, \"ept\": %d, \"blocks_per_sm\": %d, \"variant\": %d, \"us\": %.2f}",
+                 "%s\"stage_%d\": {\"tpb\": %d, \"ept\": %d, \"blocks_per_sm\": %d, \"variant\": %d, \"us\": %.2f",
                  first ? "" : ", ", st, best.tpb, best.ept, best.bpsm, best.var, 1e3 * best_ms / reps);
         report += buf;
+        if (pair_st) report += ", \"variants_us\": {" + tried + "}";
+        report += "}";
         first = false;
     }
     report += "}";

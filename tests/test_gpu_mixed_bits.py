@@ -31,7 +31,8 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(16, 16, 16), (32, 32, 32), (96, 40, 36), (33, 17, 20), (65, 24, 16), (97, 34, 18), (24, 20, 18),
           (48, 32, 96), (1, 1, 1), (40, 1, 1), (3, 2, 5), (35, 33, 37)]
 ENV_KEYS = ("AEROFLUX_FIXED_REFINEMENT_PASSES", "AEROFLUX_MG_VCYCLES", "AEROFLUX_COLD_START",
-            "AEROFLUX_MG_PER_LEVEL", "AEROFLUX_MG_PAIRS", "AEROFLUX_MG_PASS_FLOOR", "AEROFLUX_SWEEP_ROWS")
+            "AEROFLUX_MG_PER_LEVEL", "AEROFLUX_MG_PAIRS", "AEROFLUX_MG_PASS_FLOOR", "AEROFLUX_SWEEP_ROWS",
+            "AEROFLUX_PAIR_VARIANT")
 # The staged tile sweep (default) and the row sweep compute the same bits.
 SWEEPS = {"staged": {}, "rows": {"AEROFLUX_SWEEP_ROWS": 1}}
 
@@ -191,12 +192,68 @@ def test_per_level_kernels_bit_exact():
     e.Close()
 
 
-def test_batched_slots_bit_exact():
+@pytest.mark.parametrize("var", [0, 1, 2, 3])
+@pytest.mark.parametrize("n", [(96, 40, 36), (48, 32, 96), (36, 33, 37), (65, 24, 16), (128, 20, 12),
+                               (196, 20, 18)])
+def test_pair_tile_variants_bit_exact(n, var):
+    # Every tile variant of the fused pair, the TMA-staged z-march (3)
+    # included, computes the same bits: z chunks of 16 planes with ragged
+    # last chunks (nz = 36, 37, 18), ragged y tiles (ny = 33, 20), columns
+    # past the x extent (nx = 36, 48) and columns clear of both x walls
+    # (nx = 196).  Variant 3 runs on levels whose x extent is a multiple of
+    # 4 and variant 1 on the others (nx = 65, 33, ...).
+    e, o = make_mixed_pair(n, env_kw={"AEROFLUX_PAIR_VARIANT": var})
+    for k in range(2):
+        e.Step(1)
+        o.step(1)
+        assert e.LastProjectionStats()[0] == o.passes, f"step {k}"
+        assert_same(e.download, o, FIELDS, f"{n} pair variant {var} step {k}")
+    e.Close()
+
+
+def test_staged_pair_falls_back_for_a_later_slot():
+    # A slot assigned after its levels chose the staged pair but without the
+    # pair's tensor maps (nx = 66 is not a multiple of 4) switches those
+    # levels back to plain tiles; both slots keep the restatement's bits.
+    with env(AEROFLUX_PAIR_VARIANT=3):
+        b = Batch(2)
+    orcs = {}
+
+    def add(cfg, k):
+        s = b.assign(cfg)
+        o = oracle_for(b.config(s))
+        u, v, w = taylor_green(b.config(s), 1.0, 0.01, 42, k)
+        for i, (name, a) in enumerate((("U", u), ("V", v), ("W", w)), start=1):
+            b.upload(s, name, a)
+            o.data(i)[:] = a
+        o.apply_velocity_bc()
+        orcs[s] = o
+        return s
+
+    s0 = add(mixed_cfg((64, 32, 24)), 0)
+    b.apply_velocity_bc()
+    b.step(1)
+    orcs[s0].step(1)
+    s1 = add(mixed_cfg((66, 20, 16)), 1)
+    b.set_active(s0, False)
+    b.apply_velocity_bc()
+    b.set_active(s0, True)
+    b.step(2)
+    for s, o in orcs.items():
+        o.step(2)
+        assert_same(lambda name: b.download(s, name), o, FIELDS, f"slot {s}")
+    b.close()
+
+
+@pytest.mark.parametrize("pair_var", [None, 3])
+def test_batched_slots_bit_exact(pair_var):
     # Uneven slots of the batched workload's generator (the smaller ones,
-    # so the oracle stays quick) plus odd extents, stepping in one batch.
+    # so the oracle stays quick) plus odd extents, stepping in one batch
+    # (with the size-chosen pair tiles, and with the staged pair forced).
     cfgs = [c for c in batched_instances(64) if c.NX * c.NY * c.NZ <= 64 * 64 * 48][:6]
     cfgs += [mixed_cfg((33, 17, 20)), mixed_cfg((65, 24, 16), Viscosity=3e-5)]
-    b = Batch(len(cfgs))
+    with env(**({} if pair_var is None else {"AEROFLUX_PAIR_VARIANT": pair_var})):
+        b = Batch(len(cfgs))
     orcs, slots = [], []
     for k, c in enumerate(cfgs):
         s = b.assign(c)
