@@ -1230,7 +1230,7 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
 // boundary; box cells outside the level load as zeros and are never read.
 constexpr int kZmTX = 64, kZmTY = 16, kZmZC = 16, kZmBX = 72;
 constexpr int kZmEY = kZmTY + 4, kZmRY = kZmTY + 2;     // e rows: tile + 2 each side; r and red rows: + 1
-constexpr int kZmNE = 6, kZmNR = 5, kZmNRed = 4, kZmLead = 3, kZmNB = 4;
+constexpr int kZmNE = 8, kZmNR = 8, kZmNRed = 4, kZmLead = 5, kZmNB = 8;
 constexpr int kZmEBox = kZmBX * kZmEY, kZmRBox = kZmBX * kZmRY;  // floats one plane load delivers
 // Ring slots of e and r planes start on 128-byte boundaries (the rule for a
 // TMA tensor load's shared-memory destination): plane pitches round up to 32 floats.
@@ -1238,24 +1238,60 @@ constexpr int kZmEPlane = (kZmEBox + 31) / 32 * 32, kZmRPlane = (kZmRBox + 31) /
 constexpr int kZmRedPlane = kZmRY * 33;
 constexpr int kZmROff = kZmNE * kZmEPlane, kZmRedOff = kZmROff + kZmNR * kZmRPlane;  // ring offsets (floats)
 constexpr int kZmFloats = kZmRedOff + kZmNRed * kZmRedPlane;
-constexpr int kZmThreads = kZmTY * 32;
+// 18 warps: warp w computes red halo row w, warps 0-15 also the black cells
+// of tile row w and warp 16 the rows' 33rd red cells, so no warp does more
+// than two row passes between the march's barriers.  Two blocks per SM keep
+// every per-thread offset of the column in registers (with fewer, the
+// compiler re-derives them from the thread index at every step).
+constexpr int kZmWarps = kZmRY;
+constexpr int kZmThreads = kZmWarps * 32;
+constexpr int kZmBlocks = 2;
 constexpr size_t kZmSmem = (size_t)kZmFloats * sizeof(float);
 // Ring sizes for a lead of kZmLead groups with each group waited one step
 // before its first read (a slot is rewritten only after its last reader).
-static_assert(kZmNE >= kZmLead + 3 && kZmNR >= kZmLead + 2 && kZmNB >= 2, "ring sizes of the z-march");
-static_assert(kZmNRed == 4, "red ring slots are taken with & 3");
+static_assert(kZmNE >= kZmLead + 3 && kZmNR >= kZmLead + 2 && kZmNB > kZmLead, "ring sizes of the z-march");
+// The march is unrolled by 8 steps, so every ring slot, red plane and
+// barrier of a step is a compile-time constant.
+static_assert(kZmNE == 8 && kZmNR == 8 && kZmNB == 8 && kZmNRed == 4, "ring sizes of the unrolled march");
 static_assert(kZmEPlane % 32 == 0 && kZmRPlane % 32 == 0 && kZmROff % 32 == 0,
               "TMA destinations of the z-march rings on 128-byte boundaries");
 
+// Shared-memory access of the z-march: byte addresses with compile-time
+// offsets ([addr + imm]), so a neighbour costs no address arithmetic.  The
+// bounds-checking build indexes the checked ring view instead.
+#if AEROFLUX_DEBUG_BOUNDS
+using ZmAddr = int;  // float index into the rings
+#define ZM_A(i) (i)
+#define ZM_LD(a, off) S[(a) + (off)]
+#define ZM_ST(a, v) (S[(a)] = (v))
+constexpr int kZmB = 1;  // address units per float
+#else
+using ZmAddr = unsigned;  // shared-window byte address
+template <int OFF>
+__device__ __forceinline__ float zm_lds(unsigned a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(a), "n"(OFF) : "memory");
+    return v;
+}
+__device__ __forceinline__ void zm_sts(unsigned a, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+#define ZM_A(i) (sb + 4u * (unsigned)(i))
+#define ZM_LD(a, off) zm_lds<4 * (off)>(a)
+#define ZM_ST(a, v) zm_sts((a), (v))
+constexpr int kZmB = 4;
+#endif
+
 template <int ZC>
-__global__ void __launch_bounds__(kZmThreads, 3)
+__global__ void __launch_bounds__(kZmThreads, kZmBlocks)
     kb_smooth_pair_zm(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int dir, int vc, unsigned* diag) {
     if (vc_idle(ctl, tab.n, vc)) return;
     extern __shared__ __align__(128) float zsm[];
     __shared__ __align__(8) unsigned long long bar[kZmNB];
     __shared__ unsigned stop;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (smem_addr(zsm) & 127u) {  // the rings' TMA destinations need a 128-byte aligned base
+    const unsigned sb = smem_addr(zsm);
+    if (sb & 127u) {  // the rings' TMA destinations need a 128-byte aligned base
         if (tid == 0) atomicOr(diag, 4u);
         return;
     }
@@ -1266,7 +1302,9 @@ __global__ void __launch_bounds__(kZmThreads, 3)
     }
     __syncthreads();
     if (stop) return;
-    unsigned gbase = 0;  // groups issued by this block before the current column
+    // Group k of a column completes on barrier k % 8; bit b of `phase` is
+    // the parity barrier b completes next (every thread waits every group).
+    unsigned phase = 0;
     for (int item = blockIdx.x, total = tab.prefix[tab.n]; item < total; item += gridDim.x) {
         const int s = find_slot(tab.prefix, tab.n, item);
         if (mg_off(ctl[s], vc)) continue;
@@ -1276,6 +1314,7 @@ __global__ void __launch_bounds__(kZmThreads, 3)
             continue;
         }
         AF_PTR(float) S = view(zsm, (long long)kZmFloats, DK_PAIR, s);  // the three rings
+        (void)S;
         AF_PTR(float) AF_RESTRICT eout = view(dir ? L.e : L.e2, lvl_cells(L), DK_PAIR, s);
         const int nx = L.nx, ny = L.ny, nz = L.nz;
         const unsigned local = (unsigned)(item - tab.prefix[s]);
@@ -1289,8 +1328,7 @@ __global__ void __launch_bounds__(kZmThreads, 3)
         // planes 0 and 1 (z0-2, z0-1).  A plane just beyond a z wall loads
         // the wall plane; one further out is never read and not loaded.
         auto issue = [&](int k) {
-            const unsigned g = gbase + (unsigned)k;
-            unsigned long long* b = &bar[g % kZmNB];
+            unsigned long long* b = &bar[k & 7];
             const int pa = k == 0 ? 0 : k + 2, pb = k + 2;
             int ne = 0;
             for (int p = pa; p <= pb; ++p) ne += (z0 - 2 + p >= -1 && z0 - 2 + p <= nz) ? 1 : 0;
@@ -1301,10 +1339,9 @@ __global__ void __launch_bounds__(kZmThreads, 3)
             for (int p = pa; p <= pb; ++p) {
                 const int z = z0 - 2 + p;
                 if (z >= -1 && z <= nz)
-                    tma_load_3d(zsm + (p % kZmNE) * kZmEPlane, em, x0 - 4, y0 - 2, min(max(z, 0), nz - 1), b);
+                    tma_load_3d(zsm + (p & 7) * kZmEPlane, em, x0 - 4, y0 - 2, min(max(z, 0), nz - 1), b);
             }
-            if (rr)
-                tma_load_3d(zsm + kZmROff + (k % kZmNR) * kZmRPlane, inst[s].pmap + 3 * l + 2, x0 - 4, y0 - 1, rz, b);
+            if (rr) tma_load_3d(zsm + kZmROff + (k & 7) * kZmRPlane, inst[s].pmap + 3 * l + 2, x0 - 4, y0 - 1, rz, b);
         };
         // Wall fix-up of a landed e plane: the cell beyond an x or y wall
         // takes the wall cell's value (box column 4 is x = x0, box row 2 is
@@ -1314,45 +1351,43 @@ __global__ void __launch_bounds__(kZmThreads, 3)
         const bool walls = wx0 | wx1 | wy0 | wy1;
         const int gx = nx - x0 + 4, gy = ny - y0 + 2;  // box column of x = nx, box row of y = ny
         auto fill = [&](int slot) {
-            AF_PTR(float) P = S + slot * kZmEPlane;
+            const int P = slot * kZmEPlane;
             if (tid < kZmEY) {
-                if (wx0) P[tid * kZmBX + 3] = P[tid * kZmBX + 4];
-                if (wx1) P[tid * kZmBX + gx] = P[tid * kZmBX + gx - 1];
+                const ZmAddr r = ZM_A(P + tid * kZmBX);
+                if (wx0) ZM_ST(r + 3 * kZmB, ZM_LD(r, 4));
+                if (wx1) ZM_ST(r + gx * kZmB, ZM_LD(r + (gx - 1) * kZmB, 0));
             } else if (tid >= 32 && tid < 32 + kZmBX) {
-                const int c = tid - 32;
-                if (wy0) P[kZmBX + c] = P[2 * kZmBX + c];
-                if (wy1) P[gy * kZmBX + c] = P[(gy - 1) * kZmBX + c];
+                const ZmAddr c = ZM_A(P + tid - 32);
+                if (wy0) ZM_ST(c + kZmBX * kZmB, ZM_LD(c, 2 * kZmBX));
+                if (wy1) ZM_ST(c + gy * kZmBX * kZmB, ZM_LD(c + (gy - 1) * kZmBX * kZmB, 0));
             }
         };
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
-        // Red rows of this thread: halo row `warp` at cell `lane`, and an
-        // extra one (rows 16, 17 at cell lane for warps 0, 1; cell 32 of row
-        // lane for warp 2).  e box offset of the cell for parity 0, red
-        // offset, level row and level x of the cell for parity 0.
-        const int xe = warp < kZmRY - kZmTY ? 1 : (warp == kZmRY - kZmTY && lane < kZmRY ? 2 : 0);
-        const int hyB = xe == 1 ? kZmTY + warp : (xe == 2 ? lane : 0), jB = xe == 2 ? 32 : lane;
+        // Red cells of this thread: cell `lane` of halo row `warp`, and for
+        // warp 16 also cell 32 of halo row lane % 18 (lanes 18-31 repeat
+        // lanes 0-13: the same value to the same place).  Per cell: e offset
+        // for parity 0, red offset, level row + 1, level x for parity 0.
+        const bool xe = warp == kZmTY;
+        const int hyB = lane % kZmRY, jB = 32;
         const int eA = (warp + 1) * kZmBX + 3 + 2 * lane, eB = (hyB + 1) * kZmBX + 3 + 2 * jB;
         const int dA = warp * 33 + lane, dB = hyB * 33 + jB;
-        const int yA = y0 - 1 + warp, yB = y0 - 1 + hyB;
+        const int yA = y0 + warp, yB = y0 + hyB;  // level row + 1
         const int xA = x0 - 1 + 2 * lane, xB = x0 - 1 + 2 * jB;
-        // Black cells of this thread: tile row `warp`, pair x0 + 2 lane, +1.
+        // Black cells of this thread (warps 0-15): tile row `warp`, pair
+        // x0 + 2 lane, +1; computed by every lane, stored where in the level.
+        const bool bw = warp < kZmTY;
         const int by = y0 + warp;
         const bool bok = by < ny && x0 + 2 * lane < nx;
-        const int ebk = (warp + 2) * kZmBX + 2 * lane + 5;  // e box offset of the black cell when the pair starts red
-        const int rbk = kZmRedOff + (warp + 1) * 33 + lane;  // red offset of cell lane in halo row warp+1
+        const int ebk = (warp + 2) * kZmBX + 2 * lane + 5;  // e offset of the black cell when the pair starts red
+        const int rbk = (warp + 1) * 33 + lane;              // red offset of cell lane in halo row warp+1
         const long long nxy = (long long)nx * ny;
         AF_PTR(float) gp = eout + ((long long)(x0 + 2 * lane) + (long long)nx * by + nxy * z0);
         if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             for (int k = 0; k < kZmLead && k <= K + 1; ++k) issue(k);
         }
-        auto give_up = [&](int first, int last) {  // tid 0: let the transfers of groups first..last land
-            for (int j = first; j <= last && j <= K + 1; ++j) {
-                const unsigned gj = gbase + (unsigned)j;
-                mbar_wait_bounded(&bar[gj % kZmNB], (gj / kZmNB) & 1u);
-            }
-        };
-        bool failed = !mbar_wait_bounded(&bar[gbase % kZmNB], (gbase / kZmNB) & 1u);
+        bool failed = !mbar_wait_bounded(&bar[0], phase & 1u);
+        if (!failed) phase ^= 1u;
         if (walls && !failed) {
             fill(0);
             fill(1);
@@ -1361,33 +1396,42 @@ __global__ void __launch_bounds__(kZmThreads, 3)
         if (__syncthreads_or(failed ? 1 : 0)) {
             if (tid == 0) {
                 atomicOr(diag, 1u);
-                give_up(0, kZmLead - 1);
+                for (int j = 0; j < kZmLead && j <= K + 1; ++j) mbar_wait_bounded(&bar[j], (phase >> j) & 1u);
             }
             __syncthreads();
             return;
         }
-        int s0 = 0, s1 = 1, s2 = 2, s3 = 3;  // e ring slots of planes k .. k+3
-        int sr = 0, srp = kZmNR - 1;         // r ring slots of planes k, k-1
-        for (int k = 0; k <= K + 1; ++k) {
+        // Step k (k = kb + J, J the compile-time step within a block of 8):
+        // e ring slots of planes k .. k+3 are J .. J+3 (mod 8), r slots of
+        // planes z0-1+k and z0-2+k are J and J-1, the red plane is J & 3 and
+        // group k+1's barrier is J+1.
+        auto step = [&](auto Jc, int kb) -> bool {  // false: a wait gave up (the block has returned its transfers)
+            constexpr int J = decltype(Jc)::value;
+            constexpr int s0 = J & 7, s1 = (J + 1) & 7, s2 = (J + 2) & 7, s3 = (J + 3) & 7;
+            constexpr int sr = J & 7, srp = (J + 7) & 7, b1 = (J + 1) & 7;
+            const int k = kb + J;
             if (k + 1 <= K + 1) {  // group k+1, first read at step k+1
-                const unsigned g = gbase + (unsigned)(k + 1);
-                if (!failed && !mbar_wait_bounded(&bar[g % kZmNB], (g / kZmNB) & 1u)) failed = true;
+                if (!failed) {
+                    if (mbar_wait_bounded(&bar[b1], (phase >> b1) & 1u)) phase ^= 1u << b1;
+                    else failed = true;
+                }
                 if (walls && !failed) fill(s3);
             }
             const int zr = z0 - 1 + k;
-            const int zin = (unsigned)zr < (unsigned)nz ? 1 : 0;
-            const int ec = s1 * kZmEPlane, dzm = (s0 - s1) * kZmEPlane, dzp = (s2 - s1) * kZmEPlane;
-            const int drr = kZmROff + sr * kZmRPlane - ec - kZmBX;  // r cell of e offset b (r rows start one lower)
-            const int rs = kZmRedOff + (k & 3) * kZmRedPlane;
+            const bool zin = (unsigned)zr < (unsigned)nz;
+            const ZmAddr ec = ZM_A(s1 * kZmEPlane);
+            constexpr int dzm = (s0 - s1) * kZmEPlane * kZmB, dzp = (s2 - s1) * kZmEPlane * kZmB;
+            constexpr int drr = (kZmROff + sr * kZmRPlane - s1 * kZmEPlane - kZmBX) * kZmB;
+            const ZmAddr rs = ZM_A(kZmRedOff + (J & 3) * kZmRedPlane);
             if (!failed) {
-                auto red_cell = [&](int e0, int d0, int y, int x) {
-                    const int par = (y + zr + 1) & 1;
-                    const int b = ec + e0 + par;
-                    const bool in = zin && (unsigned)y < (unsigned)ny && (unsigned)(x + par) < (unsigned)nx;
-                    const float c = S[b];
-                    S[rs + d0] = in ? mg_relax(L, S[b - 1] + S[b + 1], S[b - kZmBX] + S[b + kZmBX],
-                                               S[b + dzm] + S[b + dzp], S[b + drr], inv, c)
-                                    : c;
+                auto red_cell = [&](int e0, int d0, int y1, int x) {
+                    const int par = (y1 + zr) & 1;
+                    const ZmAddr a = ec + (e0 + par) * kZmB;
+                    const bool in = zin && (unsigned)(y1 - 1) < (unsigned)ny && (unsigned)(x + par) < (unsigned)nx;
+                    const float c = ZM_LD(a, 0);
+                    const float v = mg_relax(L, ZM_LD(a, -1) + ZM_LD(a, 1), ZM_LD(a, -kZmBX) + ZM_LD(a, kZmBX),
+                                             ZM_LD(a + (ZmAddr)dzm, 0) + ZM_LD(a + (ZmAddr)dzp, 0), ZM_LD(a + (ZmAddr)drr, 0), inv, c);
+                    ZM_ST(rs + d0 * kZmB, in ? v : c);
                 };
                 red_cell(eA, dA, yA, xA);
                 if (xe) red_cell(eB, dB, yB, xB);
@@ -1395,43 +1439,56 @@ __global__ void __launch_bounds__(kZmThreads, 3)
             if (__syncthreads_or(failed ? 1 : 0)) {
                 if (tid == 0) {
                     atomicOr(diag, 1u);
-                    give_up(k + 1, k + kZmLead - 1);
+                    for (int j = k + 1; j <= k + kZmLead - 1 && j <= K + 1; ++j)  // groups issued, not yet waited
+                        mbar_wait_bounded(&bar[j & 7], (phase >> (j & 7)) & 1u);
                 }
                 __syncthreads();
-                return;
+                return false;
             }
             if (tid == 0 && k + kZmLead <= K + 1) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 issue(k + kZmLead);
             }
-            if (k >= 2 && bok) {
+            if (k >= 2 && bw) {
                 // Black cells of plane zr - 1: e ring plane k, r plane k-1,
                 // red planes k-2, k-1, k.
                 const int pr = (by + zr - 1) & 1;
-                const int eb = s0 * kZmEPlane + ebk - pr;
-                const float c = S[eb];
-                const float rv = S[kZmROff + srp * kZmRPlane + ebk - kZmBX - pr];
-                const int r1 = rbk + ((k - 1) & 3) * kZmRedPlane;
-                const int q = 1 - pr;
-                const float sx = S[r1] + S[r1 + 1];
-                const float sy = S[r1 + q - 33] + S[r1 + q + 33];
-                const float sz = S[rbk + ((k - 2) & 3) * kZmRedPlane + q] + S[rbk + (k & 3) * kZmRedPlane + q];
+                const ZmAddr eb = ZM_A(s0 * kZmEPlane + ebk - pr);
+                const float c = ZM_LD(eb, 0);
+                constexpr int drv = (kZmROff + srp * kZmRPlane - s0 * kZmEPlane - kZmBX) * kZmB;
+                const float rv = ZM_LD(eb + (ZmAddr)drv, 0);
+                const ZmAddr r1 = ZM_A(kZmRedOff + ((J + 3) & 3) * kZmRedPlane + rbk);
+                const ZmAddr h1 = r1 + (1 - pr) * kZmB;
+                constexpr int dz0 = (((J + 2) & 3) - ((J + 3) & 3)) * kZmRedPlane * kZmB;
+                constexpr int dz2 = ((J & 3) - ((J + 3) & 3)) * kZmRedPlane * kZmB;
+                const float sx = ZM_LD(r1, 0) + ZM_LD(r1, 1);
+                const float sy = ZM_LD(h1, -33) + ZM_LD(h1, 33);
+                const float sz = ZM_LD(h1 + (ZmAddr)dz0, 0) + ZM_LD(h1 + (ZmAddr)dz2, 0);
                 const float bv = mg_relax(L, sx, sy, sz, rv, inv, c);
-                const float red_v = S[r1 + pr];
-                AF_VEC(float2, gp, 0, 2) = pr ? make_float2(bv, red_v) : make_float2(red_v, bv);
+                const float red_v = ZM_LD(r1 + pr * kZmB, 0);
+                if (bok) AF_VEC(float2, gp, 0, 2) = pr ? make_float2(bv, red_v) : make_float2(red_v, bv);
             }
             if (k >= 2) gp += nxy;
-            s0 = s1;
-            s1 = s2;
-            s2 = s3;
-            s3 = s3 + 1 == kZmNE ? 0 : s3 + 1;
-            srp = sr;
-            sr = sr + 1 == kZmNR ? 0 : sr + 1;
+            return true;
+        };
+        bool ok = true;
+        for (int kb = 0; ok && kb <= K + 1; kb += 8) {
+            ok = step(std::integral_constant<int, 0>{}, kb);
+            if (ok && kb + 1 <= K + 1) ok = step(std::integral_constant<int, 1>{}, kb);
+            if (ok && kb + 2 <= K + 1) ok = step(std::integral_constant<int, 2>{}, kb);
+            if (ok && kb + 3 <= K + 1) ok = step(std::integral_constant<int, 3>{}, kb);
+            if (ok && kb + 4 <= K + 1) ok = step(std::integral_constant<int, 4>{}, kb);
+            if (ok && kb + 5 <= K + 1) ok = step(std::integral_constant<int, 5>{}, kb);
+            if (ok && kb + 6 <= K + 1) ok = step(std::integral_constant<int, 6>{}, kb);
+            if (ok && kb + 7 <= K + 1) ok = step(std::integral_constant<int, 7>{}, kb);
         }
-        gbase += (unsigned)(K + 2);
+        if (!ok) return;
         __syncthreads();  // every thread is done with the rings before the next column's loads
     }
 }
+#undef ZM_A
+#undef ZM_LD
+#undef ZM_ST
 
 // --- tail V-cycle: every level from the slot's tail down, in one block -------
 // Levels of at most kCoarseMax cells live in shared memory: pre-smoothing and
@@ -1939,7 +1996,7 @@ void launch_pair(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
 }
 
 Shape pair_shape(bool wide, int var) {
-    if (var == 3) return Shape{kZmThreads, 1, 3, 3};  // shared memory holds three z-marching blocks per SM
+    if (var == 3) return Shape{kZmThreads, 1, kZmBlocks, 3};
     const int threads = kPairVarTY[var] * (wide ? 32 : 16);
     return Shape{threads, 1, (var == 0 ? 2048 : 1536) / threads, var};
 }

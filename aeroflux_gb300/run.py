@@ -3,6 +3,7 @@
     python -m aeroflux_gb300.run --n 256 --steps 2 [--gsi 200] [--dt 0.001] [--nu 1e-5]
                                  [--precision fp64|mixed] [--project N] [--inner-sweeps K] [--warmup W]
                                  [--multigrid TOL] [--maccormack] [--batch G] [--profile-range]
+                                 [--tune-report]
 
 --project N runs N projections (BC, divergence, red-black sweeps, gradient)
 instead of Steps.  The initial field is the seeded Taylor-Green vortex with
@@ -10,7 +11,10 @@ uniform noise used by the benchmark.  --batch G steps the first G grids of
 the batched workload (extents from {32,48,64,96,128}, mixed form) in one
 tuned batch instead of one cube.  --profile-range brackets the measured
 Steps (not the set-up, tuning or warm-up) with the CUDA profiler's start and
-stop, for `ncu --profile-from-start off`.
+stop, for `ncu --profile-from-start off`.  --tune-report prints the
+autotuner's report instead of stepping (the batch's, or that of a one-slot
+batch holding the mixed-form cube): the chosen launch shape of every stage
+and, for the fused red-black pair stages, every tile variant's time.
 """
 from __future__ import annotations
 
@@ -45,7 +49,11 @@ def run_batch(a) -> None:
     cfgs = batched_instances(a.batch)
     b = Batch(len(cfgs))
     slots = [b.assign(c) for c in cfgs]
-    b.tune(2)
+    rep = b.tune(5 if a.tune_report else 2)
+    if a.tune_report:
+        print(json.dumps(rep))
+        b.close()
+        return
     for s in slots:
         b.seed(s, 1.0, a.noise, 42, s)
     b.apply_velocity_bc()
@@ -80,9 +88,19 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=0, help="step the first G grids of the batched workload")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket the measured Steps with cudaProfilerStart/Stop")
+    ap.add_argument("--tune-report", action="store_true", help="print the autotuner's report and exit")
     a = ap.parse_args()
     if a.batch:
         run_batch(a)
+        return
+    if a.tune_report:
+        from .batch import Batch
+        b = Batch(1)
+        s = b.assign(Config(NX=a.n, NY=a.n, NZ=a.n, H=1.0 / a.n, DT=a.dt, Viscosity=a.nu, Density=1.0,
+                            Precision=AF_PRECISION_MIXED, InnerSweeps=a.inner_sweeps))
+        b.seed(s, 1.0, a.noise, 42, 0)
+        print(json.dumps(b.tune(5)))
+        b.close()
         return
     prec = AF_PRECISION_MIXED if a.precision == "mixed" else AF_PRECISION_FP64
     cfg = Config(NX=a.n, NY=a.n, NZ=a.n, H=1.0 / a.n, DT=a.dt, Viscosity=a.nu, Density=1.0,
