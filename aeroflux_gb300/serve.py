@@ -126,13 +126,21 @@ def _summary(done: list[dict], censored_ages: list[float], window: float, elapse
             "worst_max_divergence": float(max((r["max_divergence"] for r in done), default=float("nan")))}
 
 
-def run_stream(requests, window: float, budget_bytes: int = 150 << 30, max_slots: int = 64,
-               max_round_steps: int = 4, device: int = 0, tune_after: int = 8,
-               max_resident_cells: int = 24 << 20, drain: bool = True) -> dict:
+def run_stream(requests, window: float, budget_bytes: int = 150 << 30, max_slots: int = 128,
+               max_round_steps: int = 8, device: int = 0, tune_after: int = 8,
+               max_resident_cells: int = 96 << 20, drain: bool = True) -> dict:
     """Replays (arrival_s, cfg, steps) in real time: requests arrive for
     `window` seconds; afterwards nothing new is admitted and, with drain,
     the requests already resident step until they finish.  Requests still
-    queued then are censored (reported with their count and age)."""
+    queued then are censored (reported with their count and age).
+
+    The default caps (96 Mi resident cells, 128 slots, 8 Steps a round)
+    trade latency for throughput: on GB300, over the 200/s benchmark stream
+    (30 s windows), executed cell-steps/s rose from 0.83 G at 24 Mi cells,
+    32 slots, 4 Steps a round to 0.93 G at 64 Mi, 0.97 G at 96 Mi and
+    0.98 G at 128 Mi / 256 slots, while the median latency of completed
+    requests rose from 21 s to 34 s (the stream is far beyond capacity, so
+    queueing dominates latency at any cap)."""
     srv = Server(budget_bytes, max_slots, device, max_round_steps, max_resident_cells=max_resident_cells)
     pending = [r for r in requests if r[0] < window]
     offered = sum(c.NX * c.NY * c.NZ * s for _, c, s in pending)

@@ -398,8 +398,8 @@ def bench_served(args, local):
     from aeroflux_gb300.serve import run_stream, run_stream_fp64
     from aeroflux_gb300.workloads import served_requests
     reqs = served_requests(200.0, args.serve_seconds, 42)
-    mixed = run_stream(reqs, args.serve_seconds, budget_bytes=150 << 30, max_slots=32, max_round_steps=4,
-                       device=local)
+    mixed = run_stream(reqs, args.serve_seconds, budget_bytes=150 << 30, max_slots=128, max_round_steps=8,
+                       max_resident_cells=96 << 20, device=local)
     fp64 = run_stream_fp64(reqs, args.serve_seconds, device=local)
     return {"mixed": mixed, "plain_fp64_sequential": fp64,
             "workload": f"Poisson arrivals at 200/s for {args.serve_seconds:g} s, extents uniform over multiples "
