@@ -125,6 +125,7 @@ struct InstDev {
     FastDiv swx, swy;        // staged sweep: spatial tiles along x and along y
     int warm;                // 1: a projection starts from the last pressure, 0: from zero
     int bc_off[10];          // velocity BC write sets: prefix of the nine (component, set) counts
+    FastDiv bcd[9][2];       // their index decoding's divisors (bc_cell_div's d1, d2)
     Lvl lev[kMaxLev];
 };
 
@@ -212,17 +213,23 @@ __global__ void kb_bc(const InstDev* inst, Status* st, Tab tab, int parity, int 
     AF_PTR(double) u = view(cur(I, 1, parity), I.g.u.count, DK_BC, s);
     AF_PTR(double) v = view(cur(I, 2, parity), I.g.v.count, DK_BC, s);
     AF_PTR(double) w = view(cur(I, 3, parity), I.g.w.count, DK_BC, s);
-    const int n = I.bc_off[9];
+    int off[10];  // the offsets in registers: no reload per element
+#pragma unroll
+    for (int j = 0; j < 10; ++j) off[j] = I.bc_off[j];
     FOR_ELEMS(tab)
-    if (el >= n) break;
+    if (el >= off[9]) break;
     // Write set k = 3 * component + set holds elements bc_off[k] ..
     // bc_off[k+1]-1 (bc_set_count in that order).
     const int e = (int)el;
-    int k = 0;
+    int k = 0, base = 0;
 #pragma unroll
-    for (int j = 1; j < 9; ++j) k += e >= I.bc_off[j] ? 1 : 0;
+    for (int j = 1; j < 9; ++j)
+        if (e >= off[j]) {
+            k = j;
+            base = off[j];
+        }
     const int comp = k / 3;
-    bc_cell(bc_comp(I.g, comp, u, v, w), I.g.G, k - 3 * comp, e - I.bc_off[k]);
+    bc_cell_div(bc_comp(I.g, comp, u, v, w), I.g.G, k - 3 * comp, (unsigned)(e - base), I.bcd[k][0], I.bcd[k][1]);
     END_ELEMS
     END_TILES
 }
@@ -2589,6 +2596,12 @@ int batch_assign(Batch* b, const af_config& c, char* arena, std::string* err) {
             for (int set = 0; set < 3; ++set) {
                 I.bc_off[3 * c + set] = (int)acc;
                 const long long Nn = N[c][0], N1 = N[c][1], N2 = N[c][2];
+                // Components 1 and 2 (V, W) have their first tangential
+                // axis along x, the stride-1 one (bc_t1_first).
+                unsigned d1, d2;
+                bc_divisors((int)Nn, (int)N1, (int)N2, c != 0 && set == 2, set, &d1, &d2);
+                I.bcd[3 * c + set][0] = FastDiv(d1);
+                I.bcd[3 * c + set][1] = FastDiv(d2);
                 acc += set == 0 ? 2 * N1 * N2 : (set == 1 ? 2 * (Nn + 1) * N2 : 2 * (Nn + 1) * (N1 + 2));
             }
         I.bc_off[9] = (int)acc;

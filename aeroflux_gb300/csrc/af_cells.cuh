@@ -206,39 +206,56 @@ __device__ __forceinline__ double bc_src(const BcComp& c, int G, int n, int a, i
     return c.f[(long long)n * c.s_n + (long long)a * c.s_1 + (long long)b * c.s_2];
 }
 
+// Divides by a divisor fixed per call (the plain 32-bit division).
+struct HwDiv {
+    unsigned d;
+    __device__ __forceinline__ unsigned div(unsigned n) const { return n / d; }
+};
+
 // Writes element i (< bc_set_count) of write set `set` of one component:
 // 0 = wall faces, 1 = ghosts of the first tangential axis, 2 = ghosts of the
 // second tangential axis (edges included).  A set holds fewer than 2^32
 // elements (2 (N+2)^2 for extents N below 46000), so the index decoding
-// divides in 32 bits.
-__device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long long il) {
-    const unsigned i = (unsigned)il;
+// divides in 32 bits.  Consecutive elements walk the axis with stride 1
+// where the set has one (set 2 of V and W walks x, the first tangential
+// axis, instead of the normal one), so a warp's stores fill whole sectors;
+// every cell is written once from cells nobody writes, so the order does not
+// change a bit.  bc_divisors gives the two divisors; D is any divider with
+// the quotients of plain division.
+__device__ __forceinline__ bool bc_t1_first(const BcComp& c, int set) { return set == 2 && c.s_1 == 1; }
+__device__ __host__ __forceinline__ void bc_divisors(int Nn, int N1, int N2, bool t1_first, int set, unsigned* d1,
+                                                     unsigned* d2) {
+    if (set == 0) *d1 = (unsigned)N1, *d2 = (unsigned)N2;
+    else if (set == 1) *d1 = (unsigned)(Nn + 1), *d2 = (unsigned)N2;
+    else if (t1_first) *d1 = (unsigned)(N1 + 2), *d2 = (unsigned)(Nn + 1);
+    else *d1 = (unsigned)(Nn + 1), *d2 = (unsigned)(N1 + 2);
+}
+template <class D>
+__device__ __forceinline__ void bc_cell_div(const BcComp& c, int G, int set, unsigned i, const D& d1, const D& d2) {
     int n, t1, t2;
     double val;
+    const unsigned r = d1.div(i), q = d2.div(r);
+    int lo = (int)(i - r * d1.d), mid = (int)(r - q * d2.d);
+    if (bc_t1_first(c, set)) {  // lo walks t1, mid the normal axis
+        const int t = lo;
+        lo = mid;
+        mid = t;
+    }
     if (set == 0) {
-        const unsigned n1 = (unsigned)c.N1, n2 = (unsigned)c.N2;
-        const unsigned r = i / n1;
-        t1 = G + (int)(i - r * n1);
-        const unsigned q = r / n2;
-        t2 = G + (int)(r - q * n2);
+        t1 = G + lo;
+        t2 = G + mid;
         n = q ? G + c.Nn : G;
         val = 0.0;
     } else if (set == 1) {
-        const unsigned nn = (unsigned)(c.Nn + 1), n2 = (unsigned)c.N2;
-        const unsigned r = i / nn;
-        n = G + (int)(i - r * nn);
-        const unsigned q = r / n2;
-        t2 = G + (int)(r - q * n2);
+        n = G + lo;
+        t2 = G + mid;
         const int side = (int)q;
         t1 = side ? G + c.N1 : G - 1;
         const int s1 = side ? G + c.N1 - 1 : G;
         val = flip(bc_src(c, G, n, s1, t2));
     } else {
-        const unsigned nn = (unsigned)(c.Nn + 1), n1 = (unsigned)(c.N1 + 2);
-        const unsigned r = i / nn;
-        n = G + (int)(i - r * nn);
-        const unsigned q = r / n1;
-        t1 = G - 1 + (int)(r - q * n1);
+        n = G + lo;
+        t1 = G - 1 + mid;
         const int side = (int)q;
         t2 = side ? G + c.N2 : G - 1;
         const int s2 = side ? G + c.N2 - 1 : G;
@@ -250,6 +267,12 @@ __device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long lo
         val = odd ? flip(s) : s;
     }
     c.f[(long long)n * c.s_n + (long long)t1 * c.s_1 + (long long)t2 * c.s_2] = val;
+}
+
+__device__ __forceinline__ void bc_cell(const BcComp& c, int G, int set, long long il) {
+    HwDiv d1, d2;
+    bc_divisors(c.Nn, c.N1, c.N2, bc_t1_first(c, set), set, &d1.d, &d2.d);
+    bc_cell_div(c, G, set, (unsigned)il, d1, d2);
 }
 
 __device__ __forceinline__ BcComp bc_comp(const Geom& g, int comp, AF_PTR(double) u, AF_PTR(double) v,
