@@ -439,7 +439,12 @@ __global__ void kb_sweep(const InstDev* inst, Status* st, Tab tab, int parity, i
 // Backtraces that leave the staged halo read the shadow in global memory
 // instead.  Every face's arithmetic is the row kernel's (mx_face_vel4,
 // mx_backtrace, mx_face_value): the same bits.
-constexpr int kSwTX = 32, kSwTY = 8, kSwTZ = 4, kSwHA = 2, kSwThreads = kSwTX * kSwTY;
+// Six planes deep: a thread computes six faces per tile, so the tile's
+// set-up (decode, slot search, geometry, transfer wait, barriers) is spread
+// over more faces than with four planes, while four blocks still fit an SM
+// (measured per sweep launch at 256^3: 4 planes 268-281 us, 6 planes
+// 236-250 us, 8 planes at three blocks per SM 290-311 us).
+constexpr int kSwTX = 32, kSwTY = 8, kSwTZ = 6, kSwHA = 2, kSwThreads = kSwTX * kSwTY;
 // Box roles: 0-2 the own component for a sweep along x, y, z; 3 the axis
 // component.  First x of a box (a multiple of 4) and its width.
 __host__ __device__ constexpr int sw_box_x(int role, int x0) {
@@ -454,8 +459,15 @@ __host__ __device__ constexpr int sw_by(int role) {
 __host__ __device__ constexpr int sw_bz(int role) {
     return role == 2 ? kSwTZ + 2 * kSwHA : (role == 3 ? kSwTZ + 2 : kSwTZ);
 }
-constexpr int kSwOwnMax = 2304;  // floats of the largest own-component box (sweep along z)
+__host__ __device__ constexpr int sw_box_floats(int role) { return sw_bx(role) * sw_by(role) * sw_bz(role); }
+__host__ __device__ constexpr int sw_max(int a, int b) { return a > b ? a : b; }
+// Floats of the largest own-component box, rounded up to 32 (128 bytes: the
+// buffers are TMA destinations).
+constexpr int kSwOwnMax = (sw_max(sw_box_floats(0), sw_max(sw_box_floats(1), sw_box_floats(2))) + 31) / 32 * 32;
 constexpr int kSwAxCount = (kSwTX + 8) * (kSwTY + 2) * (kSwTZ + 2);
+static_assert(kSwAxCount % 32 == 0, "axis-box buffers start on 128-byte boundaries");
+// Two buffer pairs (own, axis) per block, in dynamic shared memory.
+constexpr size_t kSwSmem = (size_t)2 * (kSwOwnMax + kSwAxCount) * sizeof(float);
 static_assert(sw_bx(0) * sw_by(0) * sw_bz(0) <= kSwOwnMax && sw_bx(1) * sw_by(1) * sw_bz(1) <= kSwOwnMax &&
               sw_bx(2) * sw_by(2) * sw_bz(2) <= kSwOwnMax, "own box exceeds its buffer");
 static_assert(sw_bx(3) * sw_by(3) * sw_bz(3) == kSwAxCount, "axis box size");
@@ -554,41 +566,47 @@ __device__ __forceinline__ void sweep_tile_faces(const InstDev& I, Status* st, c
     const long long py = I.shp[C], pz = py * d.ny;
     const long long gs = AX == 0 ? 1 : (AX == 1 ? py : pz);
     const float dt_invh = I.dt_invh, lam = I.lam;
-    for (int x = x0 + lx; x < xhi; x += kSwTX)
-    for (int z = z0; z < zend; ++z) {
-        const int io = ((z - oz) * BY + (y - oy)) * BX + (x - ox);
-        float vel;
-        if (C == AX) {
-            vel = own[io];
-        } else {
-            const int ia = ((z - z0 + 1) * AXY + (y - y0 + 1)) * AXX + (x - ax0);
-            // The row kernel's tap order: before the sweep axis's own
-            // component, (-e_C, 0, e_AX - e_C, e_AX); after it,
-            // (-e_C, e_AX - e_C, 0, e_AX).
-            if (AX > C) vel = mx_face_vel4(axv[ia - EC], axv[ia], axv[ia + EA - EC], axv[ia + EA]);
-            else vel = mx_face_vel4(axv[ia - EC], axv[ia + EA - EC], axv[ia], axv[ia + EA]);
+    const long long dsy = d.sy, dsz = d.sz;
+    const float* shc = I.sh[C];
+    for (int x = x0 + lx; x < xhi; x += kSwTX) {
+        // Walk z with every index advanced by its plane stride: the face's
+        // own box, the axis box and the binary64 destination.
+        int io = ((z0 - oz) * BY + (y - oy)) * BX + (x - ox);
+        int ia = (AXY + (y - y0 + 1)) * AXX + (x - ax0);
+        AF_PTR(double) dz = dd + ((long long)x + (long long)y * dsy + (long long)z0 * dsz);
+        for (int z = z0; z < zend; ++z, io += BX * BY, ia += AXX * AXY, dz += dsz) {
+            float vel;
+            if (C == AX) {
+                vel = own[io];
+            } else {
+                // The row kernel's tap order: before the sweep axis's own
+                // component, (-e_C, 0, e_AX - e_C, e_AX); after it,
+                // (-e_C, e_AX - e_C, 0, e_AX).
+                if (AX > C) vel = mx_face_vel4(axv[ia - EC], axv[ia], axv[ia + EA - EC], axv[ia + EA]);
+                else vel = mx_face_vel4(axv[ia - EC], axv[ia + EA - EC], axv[ia], axv[ia + EA]);
+            }
+            const int ca = AX == 0 ? x : (AX == 1 ? y : z);
+            int i0;
+            float t;
+            if (!mx_backtrace(vel, ca, na, dt_invh, &i0, &t)) {
+                atomicMin(&st->fault_gate, st->step * 8u + (unsigned)phase);
+                atomicMin(&st->fault_key, fault_key(C, x, y, z));
+                continue;
+            }
+            float d0, d1;
+            const int rel = i0 - ca;
+            if (i0 >= oa && i0 + 1 < oa + (AX == 0 ? BX : (AX == 1 ? BY : BZ))) {
+                d0 = own[io + rel * SO];
+                d1 = own[io + (rel + 1) * SO];
+            } else {
+                AF_PTR(const float) gp =
+                    view(shc, pz * d.nz, DK_SWEEP_TMA, slot) + (x + y * py + z * pz + rel * gs);
+                d0 = gp[0];
+                d1 = gp[gs];
+            }
+            const float res = mx_face_value(t, d0, d1, own[io - SO], own[io], own[io + SO], lam);
+            dz[0] = (double)res;  // widening is exact
         }
-        const int ca = AX == 0 ? x : (AX == 1 ? y : z);
-        int i0;
-        float t;
-        if (!mx_backtrace(vel, ca, na, dt_invh, &i0, &t)) {
-            atomicMin(&st->fault_gate, st->step * 8u + (unsigned)phase);
-            atomicMin(&st->fault_key, fault_key(C, x, y, z));
-            continue;
-        }
-        float d0, d1;
-        const int rel = i0 - ca;
-        if (i0 >= oa && i0 + 1 < oa + (AX == 0 ? BX : (AX == 1 ? BY : BZ))) {
-            d0 = own[io + rel * SO];
-            d1 = own[io + (rel + 1) * SO];
-        } else {
-            AF_PTR(const float) gp =
-                view((const float*)I.sh[C], pz * d.nz, DK_SWEEP_TMA, slot) + (x + y * py + z * pz + rel * gs);
-            d0 = gp[0];
-            d1 = gp[gs];
-        }
-        const float res = mx_face_value(t, d0, d1, own[io - SO], own[io], own[io + SO], lam);
-        dd[x + (long long)y * d.sy + (long long)z * d.sz] = (double)res;  // widening is exact
     }
 }
 
@@ -640,10 +658,16 @@ __device__ __forceinline__ void sw_issue(const InstDev& I, const SwTile& t, floa
 template <int AX>
 __global__ void __launch_bounds__(kSwThreads, 4)
     kb_sweep_tma(const InstDev* inst, Status* st, Tab tab, int parity, int phase, unsigned* diag) {
-    __shared__ __align__(128) float own[2][kSwOwnMax];
-    __shared__ __align__(128) float axv[2][kSwAxCount];
+    extern __shared__ __align__(128) float swsm[];
+    // Buffer pair k: own-component box and axis box.
+    auto own = [&](int k) { return swsm + k * kSwOwnMax; };
+    auto axv = [&](int k) { return swsm + 2 * kSwOwnMax + k * kSwAxCount; };
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ unsigned stop;
+    if (smem_addr(swsm) & 127u) {  // the buffers are TMA destinations: 128-byte aligned base
+        if (threadIdx.x == 0) atomicOr(diag, 4u);
+        return;
+    }
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -656,11 +680,11 @@ __global__ void __launch_bounds__(kSwThreads, 4)
     unsigned ph = 0u;  // bit k: the phase parity buffer k waits for next
     int item = blockIdx.x, k = 0;
     SwTile tile = sw_decode(inst, st, tab, item, total, phase);
-    if (tile.live && threadIdx.x == 0) sw_issue<AX>(inst[tile.s], tile, own[0], axv[0], &bar[0]);
+    if (tile.live && threadIdx.x == 0) sw_issue<AX>(inst[tile.s], tile, own(0), axv(0), &bar[0]);
     while (item < total) {
         const int next_item = item + gridDim.x;
         const SwTile next = sw_decode(inst, st, tab, next_item, total, phase);
-        if (next.live && threadIdx.x == 0) sw_issue<AX>(inst[next.s], next, own[k ^ 1], axv[k ^ 1], &bar[k ^ 1]);
+        if (next.live && threadIdx.x == 0) sw_issue<AX>(inst[next.s], next, own(k ^ 1), axv(k ^ 1), &bar[k ^ 1]);
         if (tile.live) {
             const bool ok = __syncthreads_and(mbar_wait_bounded(&bar[k], (ph >> k) & 1u) ? 1 : 0) != 0;
             ph ^= 1u << k;
@@ -678,10 +702,10 @@ __global__ void __launch_bounds__(kSwThreads, 4)
             const InstDev& I = inst[tile.s];
             double* dd = cur(I, 5 + tile.c, parity);
             if (tile.c == 0)
-                sweep_tile_faces<AX, 0>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
+                sweep_tile_faces<AX, 0>(I, st + tile.s, own(k), axv(k), dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
             else if (tile.c == 1)
-                sweep_tile_faces<AX, 1>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
-            else sweep_tile_faces<AX, 2>(I, st + tile.s, own[k], axv[k], dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
+                sweep_tile_faces<AX, 1>(I, st + tile.s, own(k), axv(k), dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
+            else sweep_tile_faces<AX, 2>(I, st + tile.s, own(k), axv(k), dd, tile.x0, tile.y0, tile.z0, phase, tile.s);
         }
         __syncthreads();  // every thread is done with buffer k before it is loaded again
         tile = next;
@@ -1960,9 +1984,12 @@ void enq_sweep(Batch* b, int axis, int parity, int phase, cudaStream_t s) {
     LAUNCH(b, S_SHADOW, kb_shadow, b->d_inst, tab(b, S_SHADOW), parity);
     if (b->tma_sweep) {
         const Tab t = tab(b, S_SWEEPT);
-        if (axis == 0) LAUNCH(b, S_SWEEPT, kb_sweep_tma<0>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
-        else if (axis == 1) LAUNCH(b, S_SWEEPT, kb_sweep_tma<1>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
-        else LAUNCH(b, S_SWEEPT, kb_sweep_tma<2>, b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        const int g = grid(b, S_SWEEPT);
+        if (axis == 0) kb_sweep_tma<0><<<g, kSwThreads, kSwSmem, s>>>(b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        else if (axis == 1)
+            kb_sweep_tma<1><<<g, kSwThreads, kSwSmem, s>>>(b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        else kb_sweep_tma<2><<<g, kSwThreads, kSwSmem, s>>>(b->d_inst, b->d_st, t, parity, phase, b->d_diag);
+        ++b->launches;
         return;
     }
     const Tab t = tab(b, S_SWEEP);
@@ -2350,7 +2377,10 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     // The row sweep (gathers through L1) instead of the staged tile sweep: the same bits.
     if (const char* sr = getenv("AEROFLUX_SWEEP_ROWS")) b->tma_sweep = atoi(sr) == 0;
     if (b->tma_sweep && !tensor_map_encoder()) b->tma_sweep = false;
-    b->shape[S_SWEEPT] = Shape{kSwThreads, 1, 4};
+    b->shape[S_SWEEPT] = Shape{kSwThreads, 1, 4};  // shared memory holds four blocks' buffers per SM
+    cudaFuncSetAttribute(kb_sweep_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwSmem);
+    cudaFuncSetAttribute(kb_sweep_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwSmem);
+    cudaFuncSetAttribute(kb_sweep_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwSmem);
     // Shapes: the tiny per-slot control and coarse stages keep their own.
     b->shape[S_COARSE] = Shape{kCoarseThreads, 1, 2};
     for (int l = 0; l < kMaxLev; ++l) {
