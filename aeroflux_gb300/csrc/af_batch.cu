@@ -965,7 +965,11 @@ __device__ __forceinline__ float mg_residual(const Lvl& L, int x, int y, int z, 
 
 // Coarse rhs = mean of the children's residuals; coarse solution = 0.  One
 // thread per coarse cell (row-wise forms of this kernel measured slower).
-__global__ void kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
+// 32 registers a thread (without spilling) let a whole SM's threads be
+// resident: the finest restriction at 256^3 measured 43.5 -> 37.4 us against
+// the compiler's 56 registers.  (The prolongation spills at 32 and measured
+// slower at 32 and 40.)
+__global__ void __launch_bounds__(1024, 2) kb_restrict(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
     if (vc_idle(ctl, tab.n, vc)) return;
     FOR_TILES(tab)
     if (mg_off(ctl[s], vc)) continue;
