@@ -87,6 +87,28 @@ def test_tuned_launch_shapes_do_not_change_results():
             assert np.array_equal(bits(a[s][n]), bits(b[s][n]))
 
 
+def test_tune_report_lists_every_pair_variant():
+    # The report gives each fused-pair stage its chosen variant and every
+    # variant's time; the TMA-staged z-march (3) is offered on a level whose
+    # x extent is a multiple of 4 (64 and 128 here), and the choice is the
+    # fastest of those timed.
+    b = Batch(2)
+    for c in (Config(NX=128, NY=64, NZ=48, H=1.0 / 128, DT=0.002, Viscosity=1e-4, Density=1.0,
+                     Precision=AF_PRECISION_MIXED),
+              Config(NX=64, NY=40, NZ=36, H=1.0 / 64, DT=0.002, Viscosity=1e-4, Density=1.0,
+                     Precision=AF_PRECISION_MIXED)):
+        b.assign(c)
+    rep = b.tune(2)
+    pairs = {k: v for k, v in rep.items() if "variants_us" in v}
+    assert pairs
+    for v in pairs.values():
+        times = {int(k): t for k, t in v["variants_us"].items() if t >= 0}
+        assert {0, 1, 2} <= set(times)
+        assert v["variant"] in times and times[v["variant"]] == min(times.values())
+    assert any("3" in v["variants_us"] for v in pairs.values())
+    b.close()
+
+
 def test_slots_come_and_go_between_steps():
     b = Batch(4)
     first = [b.assign(c) for c in SHAPES[:3]]
