@@ -84,6 +84,11 @@ struct orc_engine {
     int cur_axis;
     double cur_dt;
     int cur_color;
+
+    /* MacCormack advection (orc_set_advection): scheme and the forward
+     * step's three scratch fields, laid out as U, V, W. */
+    int advection;
+    double* mc[3];
 };
 
 /* ------------------------------------------------------------------------ */
@@ -429,16 +434,16 @@ static inline int sample_trilinear(const orc_field* f, const double* d, double p
     return 0;
 }
 
-/* advectComponent, stencil.go:44-119. */
-static int advect_component(orc_engine* e, const shard* s, int src_id, int dst_id, int c, int ax, double dt,
-                            char* msg, size_t msglen) {
+/* advectComponent, stencil.go:44-119, into dd (laid out as dst); with
+ * diffuse = 0 the diffusion term is skipped (lam = 0: the MacCormack forward
+ * step). */
+static int advect_component_into(orc_engine* e, const shard* s, int src_id, double* dd, const orc_field* dst,
+                                 int c, int ax, double dt, int diffuse, char* msg, size_t msglen) {
     const orc_field* src = &e->f[src_id];
-    const orc_field* dst = &e->f[dst_id];
     double h = e->H;
     double invH = 1.0 / h;
     double nu = e->cfg.viscosity;
     const double* sd = D(e, src_id);
-    double* dd = D(e, dst_id);
     int64_t g = e->G;
     int64_t x0 = g, x1 = g + e->NX;
     int64_t y0 = g, y1 = g + e->NY;
@@ -449,7 +454,7 @@ static int advect_component(orc_engine* e, const shard* s, int src_id, int dst_i
     default:
         if (s->z1 == g + e->NZ) z1++;
     }
-    double lam = nu * dt * invH * invH;
+    double lam = diffuse ? nu * dt * invH * invH : 0.0;
     for (int64_t z = z0; z < z1; ++z) {
         for (int64_t y = y0; y < y1; ++y) {
             int64_t base = IX(src, 0, y, z);
@@ -482,6 +487,11 @@ static int advect_component(orc_engine* e, const shard* s, int src_id, int dst_i
     return 0;
 }
 
+static int advect_component(orc_engine* e, const shard* s, int src_id, int dst_id, int c, int ax, double dt,
+                            char* msg, size_t msglen) {
+    return advect_component_into(e, s, src_id, D(e, dst_id), &e->f[dst_id], c, ax, dt, 1, msg, msglen);
+}
+
 /* advectDiffuseAxis, stencil.go:21-25: a fault in one component aborts the
  * rest of the shard's work, as the panic would. */
 static int sweep_fn(orc_engine* e, const shard* s, char* msg, size_t msglen) {
@@ -489,6 +499,100 @@ static int sweep_fn(orc_engine* e, const shard* s, char* msg, size_t msglen) {
     if (advect_component(e, s, ORC_V, ORC_TMP1, COMP_V, e->cur_axis, e->cur_dt, msg, msglen)) return 1;
     if (advect_component(e, s, ORC_W, ORC_TMP2, COMP_W, e->cur_axis, e->cur_dt, msg, msglen)) return 1;
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* MacCormack advection: the engine's optional higher-order sweep (Selle,    */
+/* Fedkiw, Kim, Liu, Rossignac, J. Sci. Comput. 2008), restated in the       */
+/* binary64 operation order of the engine's kernel, one sweep axis at a time: */
+/* the forward step is the reference sweep without diffusion into scratch    */
+/* (phi^); each face then traces its velocity forward through phi^ (taps     */
+/* outside the faces the sweep writes read phi), forms phi^ + (phi - phi~)/2, */
+/* falls back to phi^ outside the range of the two source values the forward */
+/* step interpolated, and adds the reference's diffusion of phi.             */
+/* ------------------------------------------------------------------------ */
+static int mc_forward_fn(orc_engine* e, const shard* s, char* msg, size_t msglen) {
+    for (int c = 0; c < 3; ++c)
+        if (advect_component_into(e, s, ORC_U + c, e->mc[c], &e->f[ORC_U + c], c, e->cur_axis, e->cur_dt, 0, msg,
+                                  msglen))
+            return 1;
+    return 0;
+}
+
+static void maccormack_component(orc_engine* e, const shard* s, int c, int ax, double dt) {
+    const orc_field* src = &e->f[ORC_U + c];
+    const orc_field* dst = &e->f[ORC_TMP0 + c];
+    const double* sd = D(e, ORC_U + c);
+    const double* fd = e->mc[c];
+    double* dd = D(e, ORC_TMP0 + c);
+    double invH = 1.0 / e->H;
+    double lam = e->cfg.viscosity * dt * invH * invH;
+    int64_t g = e->G;
+    int64_t x1 = g + e->NX + (c == COMP_U), y1 = g + e->NY + (c == COMP_V);
+    int64_t z0 = s->z0, z1 = s->z1;
+    if (c == COMP_W && s->z1 == g + e->NZ) z1++;
+    /* the faces the sweep writes along the axis: lo .. hi */
+    int64_t lo = g, hi = ax == AXIS_X ? x1 - 1 : (ax == AXIS_Y ? y1 - 1 : g + e->NZ + (c == COMP_W) - 1);
+    int64_t step = ax == AXIS_X ? 1 : (ax == AXIS_Y ? src->sy : src->sz);
+    int64_t na = ax == AXIS_X ? src->nx : (ax == AXIS_Y ? src->ny : src->nz);
+    double maxA = (double)(na - 1);
+    for (int64_t z = z0; z < z1; ++z)
+        for (int64_t y = g; y < y1; ++y)
+            for (int64_t x = g; x < x1; ++x) {
+                int64_t i = IX(src, x, y, z);
+                double fwd = fd[i];
+                double lap = 0.0;
+                if (lam != 0) lap = lam * (sd[i - step] - 2 * sd[i] + sd[i + step]);
+                double shift = dt * face_velocity_axis(e, c, ax, x, y, z) * invH;
+                int64_t ca = ax == AXIS_X ? x : (ax == AXIS_Y ? y : z);
+                double pf = (double)ca - shift, pb = (double)ca + shift;
+                if (isnan(pf) || isnan(pb)) {
+                    dd[IX(dst, x, y, z)] = fwd + lap;
+                    continue;
+                }
+                pf = fmin(fmax(pf, 0.0), maxA);
+                pb = fmin(fmax(pb, 0.0), maxA);
+                int64_t f0 = (int64_t)pf, b0 = (int64_t)pb;
+                if (f0 >= na - 1) f0 = na - 2;
+                if (b0 >= na - 1) b0 = na - 2;
+                int64_t base = i - ca * step;
+                double s0 = sd[base + f0 * step], s1 = sd[base + (f0 + 1) * step];
+                double mn = fmin(s0, s1), mx = fmax(s0, s1);
+                double h0 = (b0 >= lo && b0 <= hi) ? fd[base + b0 * step] : sd[base + b0 * step];
+                double h1 = (b0 + 1 >= lo && b0 + 1 <= hi) ? fd[base + (b0 + 1) * step] : sd[base + (b0 + 1) * step];
+                double tb = pb - (double)b0;
+                double back = h0 * (1.0 - tb) + h1 * tb;
+                double out = fwd + 0.5 * (sd[i] - back);
+                if (!(out >= mn && out <= mx)) out = fwd;
+                dd[IX(dst, x, y, z)] = out + lap;
+            }
+}
+
+static int mc_correct_fn(orc_engine* e, const shard* s, char* msg, size_t msglen) {
+    (void)msg;
+    (void)msglen;
+    for (int c = 0; c < 3; ++c) maccormack_component(e, s, c, e->cur_axis, e->cur_dt);
+    return 0;
+}
+
+int orc_set_advection(orc_engine* e, int scheme) {
+    if (scheme != ORC_ADVECTION_SEMI_LAGRANGIAN && scheme != ORC_ADVECTION_MACCORMACK) return -1;
+    if (scheme == ORC_ADVECTION_MACCORMACK && !e->mc[0])
+        for (int c = 0; c < 3; ++c) {
+            e->mc[c] = (double*)calloc((size_t)e->f[ORC_U + c].count, sizeof(double));
+            if (!e->mc[c]) return -1;
+        }
+    e->advection = scheme;
+    return 0;
+}
+
+/* One axis sweep of the current scheme into Tmp (before commitVelocity). */
+static int sweep_phase(orc_engine* e, char* err, size_t errlen) {
+    if (e->advection == ORC_ADVECTION_MACCORMACK) {
+        if (dispatch(e, mc_forward_fn, err, errlen)) return -1;
+        return dispatch(e, mc_correct_fn, err, errlen);
+    }
+    return dispatch(e, sweep_fn, err, errlen);
 }
 
 /* commitVelocity, stencil.go:230-235: descriptor swap. */
@@ -713,7 +817,7 @@ int orc_project(orc_engine* e, char* err, size_t errlen) {
 int orc_sweep(orc_engine* e, int axis, double dt, char* err, size_t errlen) {
     e->cur_axis = axis;
     e->cur_dt = dt;
-    if (dispatch(e, sweep_fn, err, errlen)) return -1;
+    if (sweep_phase(e, err, errlen)) return -1;
     commit_velocity(e);
     return 0;
 }
@@ -726,14 +830,14 @@ int orc_step(orc_engine* e, char* err, size_t errlen) {
     for (int k = 0; k < 3; ++k) {
         orc_apply_velocity_bc(e);
         e->cur_axis = fwd[k];
-        if (dispatch(e, sweep_fn, err, errlen)) return -1;
+        if (sweep_phase(e, err, errlen)) return -1;
         commit_velocity(e);
     }
     if (orc_project(e, err, errlen)) return -1;
     for (int k = 0; k < 3; ++k) {
         orc_apply_velocity_bc(e);
         e->cur_axis = rev[k];
-        if (dispatch(e, sweep_fn, err, errlen)) return -1;
+        if (sweep_phase(e, err, errlen)) return -1;
         commit_velocity(e);
     }
     if (orc_project(e, err, errlen)) return -1;
@@ -986,6 +1090,7 @@ void orc_close(orc_engine* e) {
     free(e->threads);
     free(e->shards);
     free(e->slots);
+    for (int c = 0; c < 3; ++c) free(e->mc[c]);
     free(e);
 }
 

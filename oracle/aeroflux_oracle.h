@@ -66,6 +66,11 @@ double* orc_field_data(orc_engine* e, int id, orc_field* desc);
 /* Whole arena (layout of grid.go:101-134), MACBytes long. */
 unsigned char* orc_arena(orc_engine* e, int64_t* bytes);
 
+/* Advection scheme of the sweeps (the engine's SetAdvection): 0 the
+ * reference's semi-Lagrangian sweep, 1 MacCormack.  0 or -1. */
+enum { ORC_ADVECTION_SEMI_LAGRANGIAN = 0, ORC_ADVECTION_MACCORMACK = 1 };
+int orc_set_advection(orc_engine* e, int scheme);
+
 /* Step, aeroflux.go:348-409.  0 or -1 with the first contained fault in err. */
 int orc_step(orc_engine* e, char* err, size_t errlen);
 /* project, project.go:12-34 (the reference's tests call it directly). */

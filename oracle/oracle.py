@@ -98,6 +98,8 @@ def lib():
         L.orc_commit_velocity.restype = None
         L.orc_seed_taylor_green.argtypes = [E, C.c_double, C.c_double, C.c_uint64, C.c_uint64]
         L.orc_seed_taylor_green.restype = None
+        L.orc_set_advection.argtypes = [E, C.c_int]
+        L.orc_set_advection.restype = C.c_int
         L.orc_set_mutation.argtypes = [C.c_int]
         L.orc_set_mutation.restype = None
         L.orc_go_format_float.argtypes = [C.c_double, C.c_char_p, C.c_size_t]
@@ -203,6 +205,11 @@ class OracleEngine:
 
     def sweep(self, axis: int, dt: float):
         self._err_call(lib().orc_sweep, axis, dt)
+
+    def set_advection(self, scheme: int):
+        """0: the reference's semi-Lagrangian sweeps; 1: MacCormack."""
+        if lib().orc_set_advection(self._h, scheme) != 0:
+            raise OracleError(f"orc_set_advection({scheme}) failed")
 
     def commit_velocity(self):
         lib().orc_commit_velocity(self._h)
