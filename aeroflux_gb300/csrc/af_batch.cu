@@ -1254,16 +1254,17 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
 // neighbour: the black pass needs no selects either.  Arithmetic and operand
 // order are those of kb_smooth_pair: the same bits.
 //
-// Every thread keeps its rows for the whole column: warp w computes the red
-// cells of halo row w (warps 0, 1 also rows 16, 17; warp 2 the rows' 33rd
-// cells) and the black cells of tile row w.  A plane's loads are waited one
-// step before it is first read, so its wall fix-up is published by the
-// step's one block barrier.
+// Every thread keeps its rows for the whole column: warp w of 18 computes
+// the red cells of halo row w (warp 16 also the rows' 33rd cells) and warps
+// 0-15 the black cells of tile row w.  Plane loads run five steps ahead; a
+// plane's loads are waited one step before it is first read, so its wall
+// fix-up is published by the step's one block barrier.
 //
 // A level runs it only when its rows and arrays are 16-byte aligned (nx a
 // multiple of 4; InstDev::pmap, Lvl::tma).  Boxes start at x0 - 4, a 16-byte
 // boundary; box cells outside the level load as zeros and are never read.
 constexpr int kZmTX = 64, kZmTY = 16, kZmZC = 16, kZmBX = 72;
+static_assert(kPairVarTY[3] == kZmTY && kPairVarTZ[3] == kZmZC, "work-list tiles of pair variant 3");
 constexpr int kZmEY = kZmTY + 4, kZmRY = kZmTY + 2;     // e rows: tile + 2 each side; r and red rows: + 1
 constexpr int kZmNE = 8, kZmNR = 8, kZmNRed = 4, kZmLead = 5, kZmNB = 8;
 constexpr int kZmEBox = kZmBX * kZmEY, kZmRBox = kZmBX * kZmRY;  // floats one plane load delivers
