@@ -1135,13 +1135,16 @@ __device__ float block_sum(float v, float* red) {
 // autotuner picks a variant per level; untuned, the level's size does.
 // Variant 3 is the TMA-staged z-marching pair (kb_smooth_pair_zm): 64 x 16
 // columns of 16 planes.
-constexpr int kPairVarTY[4] = {16, 8, 4, 16}, kPairVarTZ[4] = {8, 4, 4, 16};
+// Variant 4: 64 x 16 x 16 tiles, the red halo recomputed over 1.27x the
+// tile's red cells.
+constexpr int kPairVarTY[5] = {16, 8, 4, 16, 16}, kPairVarTZ[5] = {8, 4, 4, 16, 16};
 constexpr int kPairWideX = 64;
 
 template <int LANES, int V>
 struct PairTile {
-    static constexpr int TY = V == 0 ? 16 : (V == 1 ? 8 : 4);
-    static constexpr int TZ = V == 0 ? 8 : 4;
+    static constexpr int TY = kPairVarTY[V];
+    static constexpr int TZ = kPairVarTZ[V];
+    static constexpr int FY = V == 4 ? 0 : V;  // Lvl::fty entry of TY
     static constexpr int HY = TY + 2, HZ = TZ + 2;
     static constexpr int TX = 2 * LANES;        // cells along x
     static constexpr int RX = LANES + 1;        // red cells of a halo row
@@ -1150,7 +1153,7 @@ struct PairTile {
     // Resident threads per SM the launch bounds ask for: all 2048 for the
     // largest tiles (32 registers suffice), 1536 for the others (their
     // index arithmetic would spill at 32).
-    static constexpr int RESIDENT = V == 0 ? 2048 : 1536;
+    static constexpr int RESIDENT = V == 0 || V == 4 ? 2048 : 1536;
 };
 
 template <int LANES, int V>
@@ -1173,14 +1176,14 @@ __global__ void __launch_bounds__(PairTile<LANES, V>::THREADS, PairTile<LANES, V
         const unsigned local = (unsigned)(item - tab.prefix[s]);
         int x0, y0, z0;
         if (LANES == 32) {
-            const unsigned q1 = L.ftx.div(local), q2 = L.fty[V].div(q1);
+            const unsigned q1 = L.ftx.div(local), q2 = L.fty[T::FY].div(q1);
             x0 = (int)(local - q1 * L.ftx.d) * T::TX;
-            y0 = (int)(q1 - q2 * L.fty[V].d) * T::TY;
+            y0 = (int)(q1 - q2 * L.fty[T::FY].d) * T::TY;
             z0 = (int)q2 * T::TZ;
         } else {
-            const unsigned q2 = L.fty[V].div(local);
+            const unsigned q2 = L.fty[T::FY].div(local);
             x0 = L.nxw;
-            y0 = (int)(local - q2 * L.fty[V].d) * T::TY;
+            y0 = (int)(local - q2 * L.fty[T::FY].d) * T::TY;
             z0 = (int)q2 * T::TZ;
         }
         const float inv = 1.0f / (2.0f * (L.wx + L.wy + L.wz));
@@ -2030,14 +2033,15 @@ void launch_pair(Batch* b, int st, int l, int dir, int vc, cudaStream_t s) {
     switch (b->shape[st].var) {
         case 0: wide ? launch_pair_v<32, 0>(b, st, l, dir, vc, s) : launch_pair_v<16, 0>(b, st, l, dir, vc, s); break;
         case 1: wide ? launch_pair_v<32, 1>(b, st, l, dir, vc, s) : launch_pair_v<16, 1>(b, st, l, dir, vc, s); break;
-        default: wide ? launch_pair_v<32, 2>(b, st, l, dir, vc, s) : launch_pair_v<16, 2>(b, st, l, dir, vc, s);
+        case 2: wide ? launch_pair_v<32, 2>(b, st, l, dir, vc, s) : launch_pair_v<16, 2>(b, st, l, dir, vc, s); break;
+        default: wide ? launch_pair_v<32, 4>(b, st, l, dir, vc, s) : launch_pair_v<16, 4>(b, st, l, dir, vc, s);
     }
 }
 
 Shape pair_shape(bool wide, int var) {
     if (var == 3) return Shape{kZmThreads, 1, kZmBlocks, 3};
     const int threads = kPairVarTY[var] * (wide ? 32 : 16);
-    return Shape{threads, 1, (var == 0 ? 2048 : 1536) / threads, var};
+    return Shape{threads, 1, (var == 0 || var == 4 ? 2048 : 1536) / threads, var};
 }
 
 // Whether a used slot has wide pair tiles at level l without the staged
@@ -2411,9 +2415,9 @@ Batch* batch_create(int capacity, size_t pool_bytes, std::string* err) {
     b->h_tmaps.assign(12 * (size_t)capacity, CUtensorMap{});
     b->h_pmaps.assign(3 * kMaxLev * (size_t)capacity, CUtensorMap{});
     cudaFuncSetAttribute(kb_smooth_pair_zm<kZmZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZmSmem);
-    // The fused pairs' tile variant for every level (0-2; 3: TMA-staged where
-    // the levels allow it), instead of the tuned or size-based choice.
-    if (const char* pv = getenv("AEROFLUX_PAIR_VARIANT")) b->force_pair_var = std::min(3, std::max(0, atoi(pv)));
+    // The fused pairs' tile variant for every level (0-2 and 4; 3: TMA-staged
+    // where the levels allow it), instead of the tuned or size-based choice.
+    if (const char* pv = getenv("AEROFLUX_PAIR_VARIANT")) b->force_pair_var = std::min(4, std::max(0, atoi(pv)));
     if (pool_bytes) {
         if (!b->pool.init(pool_bytes)) {
             *err = "aeroflux: batch device pool of " + std::to_string(pool_bytes) + " bytes: out of memory";
@@ -3088,8 +3092,8 @@ std::string batch_tune(Batch* b, int reps) {
     }
     default_pair_variants(b);
     b->pair_chosen = true;
-    const Shape pair_cands[2][3] = {{pair_shape(true, 0), pair_shape(true, 1), pair_shape(true, 2)},
-                                    {pair_shape(false, 0), pair_shape(false, 1), pair_shape(false, 2)}};
+    const Shape pair_cands[2][4] = {{pair_shape(true, 0), pair_shape(true, 1), pair_shape(true, 2), pair_shape(true, 4)},
+                                    {pair_shape(false, 0), pair_shape(false, 1), pair_shape(false, 2), pair_shape(false, 4)}};
     for (int st : stages) {
         long long items = 0;
         for (auto& S : b->slots) items += stage_items(S, st, b->shape[st]);
@@ -3100,7 +3104,7 @@ std::string batch_tune(Batch* b, int reps) {
         if (pair_st && b->force_pair_var >= 0) continue;
         std::vector<Shape> cs(cands, cands + sizeof cands / sizeof cands[0]);
         if (pair_st) {
-            cs.assign(pair_cands[st >= S_PAIRN], pair_cands[st >= S_PAIRN] + 3);
+            cs.assign(pair_cands[st >= S_PAIRN], pair_cands[st >= S_PAIRN] + 4);
             if (st < S_PAIRN && pair_tma_ok(b, st - S_PAIR)) cs.push_back(pair_shape(true, 3));
         }
         std::string tried;  // fused-pair stages: every tile variant's time

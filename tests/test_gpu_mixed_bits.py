@@ -192,7 +192,7 @@ def test_per_level_kernels_bit_exact():
     e.Close()
 
 
-@pytest.mark.parametrize("var", [0, 1, 2, 3])
+@pytest.mark.parametrize("var", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("n", [(96, 40, 36), (48, 32, 96), (36, 33, 37), (65, 24, 16), (128, 20, 12),
                                (196, 20, 18)])
 def test_pair_tile_variants_bit_exact(n, var):
