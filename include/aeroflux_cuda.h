@@ -282,7 +282,10 @@ int af_batch_max_divergence(af_batch* b, int64_t slot, double* out);
 int af_batch_projection_stats(af_batch* b, int64_t slot, int64_t* passes, double* max_div);
 /* Autotuner: times candidate launch shapes of every stage on the current
  * slots (run before uploading fields or between steps) and keeps the
- * fastest; writes a JSON report.  Results are bit-identical under any shape. */
+ * fastest; writes a JSON report, per stage "stage_<n>": {"tpb", "ept",
+ * "blocks_per_sm", "variant", "us"}, and for the fused red-black pair
+ * stages also "variants_us": every tile variant's time.  Results are
+ * bit-identical under any shape or variant. */
 int af_batch_tune(af_batch* b, int32_t reps, char* report, size_t len);
 int af_batch_profile(af_batch* b, int enable);
 int af_batch_last_step_profile(af_batch* b, af_step_profile* out);
