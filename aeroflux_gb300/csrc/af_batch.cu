@@ -3048,9 +3048,9 @@ std::string batch_tune(Batch* b, int reps) {
                            {128, 4, 16}, {256, 1, 16}, {512, 2, 4}, {1024, 1, 2}};
     std::string report = "{";
     for (int& gz : b->grid_sz) gz = 0;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    reps = std::max(1, reps);
+    std::vector<cudaEvent_t> rev(2 * (size_t)reps);
+    for (auto& ev : rev) cudaEventCreate(&ev);
     cudaStream_t s = b->stream;
     // The control records must see the slots as they are now (a slot
     // assigned since the last upload would read as inactive, and every
@@ -3112,12 +3112,18 @@ std::string batch_tune(Batch* b, int reps) {
             b->shape[st] = c;
             upload_tables(b);
             run(st);  // warm-up
-            cudaEventRecord(e0, s);
-            for (int r = 0; r < reps; ++r) run(st);
-            cudaEventRecord(e1, s);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
+            // Each repetition timed on its own; the median of them stands
+            // for the candidate (one disturbed launch does not decide).
+            for (int r = 0; r < reps; ++r) {
+                cudaEventRecord(rev[2 * r], s);
+                run(st);
+                cudaEventRecord(rev[2 * r + 1], s);
+            }
+            cudaEventSynchronize(rev[2 * reps - 1]);
+            std::vector<float> t(reps);
+            for (int r = 0; r < reps; ++r) cudaEventElapsedTime(&t[r], rev[2 * r], rev[2 * r + 1]);
+            std::nth_element(t.begin(), t.begin() + reps / 2, t.end());
+            const float ms = t[reps / 2] * reps;  // per-launch median, scaled like the report's sum
             const bool ok = cudaGetLastError() == cudaSuccess;
             if (ok && ms < best_ms) {
                 best_ms = ms;
@@ -3140,8 +3146,7 @@ std::string batch_tune(Batch* b, int reps) {
         first = false;
     }
     report += "}";
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (auto& ev : rev) cudaEventDestroy(ev);
     upload_tables(b);
     kb_init<<<1, 256, 0, s>>>(b->d_inst, b->d_ctl, b->cap);
     if (b->graph) {
