@@ -1042,9 +1042,17 @@ __host__ __device__ inline int prolong_lanes_log(const Lvl& F, const Lvl& C) {
     const int w = F.cx ? C.nx : F.nx;  // lane iterations of a row
     return w > 16 ? 5 : (w > 8 ? 4 : 3);
 }
+// Where every axis coarsens, a work row is a coarse row (Y0, Z0) and covers
+// the four fine rows (2 Y0 + {0, 1}, 2 Z0 + {0, 1}), which share the coarse
+// rows Y0 - 1 .. Y0 + 1 x Z0 - 1 .. Z0 + 1: 27 coarse loads per 8 fine
+// cells instead of 48.  Otherwise a work row is a fine row.
+__host__ __device__ inline bool prolong_blocks(const Lvl& F) { return F.cx && F.cy && F.cz; }
+__host__ __device__ inline long long prolong_rows(const Lvl& F, const Lvl& C) {
+    return prolong_blocks(F) ? (long long)C.ny * C.nz : (long long)F.ny * F.nz;
+}
 __host__ __device__ inline long long prolong_box(const Lvl& F, const Lvl& C) {
     const int sh = 5 - prolong_lanes_log(F, C);
-    return 32ll * ((((long long)F.ny * F.nz) + (1 << sh) - 1) >> sh);
+    return 32ll * ((prolong_rows(F, C) + (1 << sh) - 1) >> sh);
 }
 
 __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, int vc) {
@@ -1053,12 +1061,58 @@ __global__ void kb_prolong(const InstDev* inst, const Ctl* ctl, Tab tab, int l, 
     if (mg_off(ctl[s], vc)) continue;
     const Lvl F = inst[s].lev[l];
     const Lvl C = inst[s].lev[l + 1];
-    const long long rows = (long long)F.ny * F.nz;
+    const long long rows = prolong_rows(F, C);
     const int lg = prolong_lanes_log(F, C), lanes = 1 << lg;
     FOR_ELEMS(tab)
     const long long row = ((el >> 5) << (5 - lg)) + ((el & 31) >> lg);
     if (row >= rows) break;
     const int lane = (int)(el & (lanes - 1));
+    if (prolong_blocks(F)) {
+        // Coarse rows Ym, Y0, Yp x Zm, Z0, Zp (clamped at the walls, as the
+        // fine rows' neighbours are); fine row (2 Y0 + b, 2 Z0 + c) takes
+        // neighbour row Yp if b else Ym, and plane Zp if c else Zm.
+        const unsigned cz = C.fny.div((unsigned)row);
+        const int Y0 = (int)((unsigned)row - cz * (unsigned)C.ny), Z0 = (int)cz;
+        const int Ys[3] = {max(Y0 - 1, 0), Y0, min(Y0 + 1, C.ny - 1)};
+        const int Zs[3] = {max(Z0 - 1, 0), Z0, min(Z0 + 1, C.nz - 1)};
+        AF_PTR(const float) ce = view((const float*)C.e, lvl_cells(C), DK_PROLONG, s);
+        AF_PTR(float) fe = view(F.e, lvl_cells(F), DK_PROLONG, s);
+        int co[3][3];  // coarse row offsets [z][y]
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) co[a][b] = (int)lidx(0, Ys[b], Zs[a], C.nx, C.ny);
+        int fo[2][2];  // fine row offsets [c][b]
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) fo[c][b] = (int)lidx(0, 2 * Y0 + b, 2 * Z0 + c, F.nx, F.ny);
+        for (int X = lane; X < C.nx; X += lanes) {
+            const int Xm = max(X - 1, 0), Xp = min(X + 1, C.nx - 1);
+            float a0[3][3], am[3][3], ap[3][3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    a0[a][b] = ce[co[a][b] + X];
+                    am[a][b] = ce[co[a][b] + Xm];
+                    ap[a][b] = ce[co[a][b] + Xp];
+                }
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const int y1 = b ? 2 : 0, z1 = c ? 2 : 0;  // the neighbour row and plane
+                    float2 f = AF_VEC(float2, fe, fo[c][b] + 2 * X, 2);
+                    f.x = __fadd_rn(f.x, mg_interp(0.75f, 0.75f, 0.75f, a0[1][1], am[1][1], a0[1][y1], am[1][y1],
+                                                   a0[z1][1], am[z1][1], a0[z1][y1], am[z1][y1]));
+                    f.y = __fadd_rn(f.y, mg_interp(0.75f, 0.75f, 0.75f, a0[1][1], ap[1][1], a0[1][y1], ap[1][y1],
+                                                   a0[z1][1], ap[z1][1], a0[z1][y1], ap[z1][y1]));
+                    AF_VEC(float2, fe, fo[c][b] + 2 * X, 2) = f;
+                }
+        }
+        continue;
+    }
     const unsigned zz = F.fny.div((unsigned)row);
     const int y = (int)((unsigned)row - zz * (unsigned)F.ny), z = (int)zz;
     int Y0 = y, Y1 = y, Z0 = z, Z1 = z;
