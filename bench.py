@@ -113,19 +113,27 @@ class ClockSampler:
             self.proc.kill()
         self.f.flush()
         self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        text = self.f.read()
         self.f.close()
         os.unlink(self.f.name)
-        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
-        ids = {r[0] for r in rows}
-        if len(ids) > 1:
-            rows = [r for r in rows if r[0] == str(self.idx)]
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+        return parse_clocks(text, self.idx)
+
+
+def parse_clocks(text: str, gpu_index: int) -> dict:
+    """Median SM clock, maximum clock and the throttle reasons seen in the
+    sampler's CSV (ClockSampler.Q, no header, no units); with several GPUs
+    in the samples, only gpu_index's rows count."""
+    rows = [r.split(",") for r in text.strip().splitlines() if r.strip()]
+    rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+    ids = {r[0] for r in rows}
+    if len(ids) > 1:
+        rows = [r for r in rows if r[0] == str(gpu_index)]
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(rows)}
 
 
 def measured_peaks() -> tuple[float, str]:
