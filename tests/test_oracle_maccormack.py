@@ -73,3 +73,18 @@ def test_switching_back_gives_the_reference_bits():
             return [o.data(f).copy() for f in (U, V, W, 0)]
     for a, b in zip(run(False), run(True)):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_same_bits_for_any_worker_count():
+    # The forward step and the correction run over the same z shards as the
+    # reference sweep; the result does not depend on how many there are.
+    def run(workers):
+        with OracleEngine(nx=12, ny=12, nz=12, h=1 / 12, dt=0.004, viscosity=1e-5, workers=workers) as o:
+            o.seed_taylor_green(1.0, 0.01, 42, 0)
+            o.apply_velocity_bc()
+            o.set_advection(MACCORMACK)
+            o.step(2)
+            return np.concatenate([o.data(f).copy() for f in (U, V, W, 0)])
+    ref = run(1)
+    for w in (2, 3, 4, 8):
+        assert np.array_equal(ref.view(np.uint64), run(w).view(np.uint64)), f"workers={w}"
